@@ -1,0 +1,269 @@
+/*
+ * vmc_gb300.h -- C ABI of the GB300-native (sm_103a) VMC hot path.
+ *
+ * Each entry point replaces one stage of jVMC 1.5.8's per-step hot path
+ * (the reference file:line it replaces is given with each declaration; paths
+ * are relative to the jVMC project root).  The reference is JAX code: these
+ * are the functions a jax.ffi / ctypes binding of that path calls.
+ *
+ * Conventions
+ *   - every pointer is a DEVICE pointer unless stated otherwise; the caller
+ *     owns every buffer, nothing is allocated inside an entry point;
+ *   - complex numbers are interleaved (re, im) pairs: "c128" = 2 doubles
+ *     (numpy complex128 / jnp.complex128), "c64" = 2 floats;
+ *   - configurations are int32 with values in [0, local_dim), row-major
+ *     (num_configs, num_sites), the layout of jVMC's samplers
+ *     (sampler.py:118-121, 320-323);
+ *   - all work is stream-ordered on `stream` (a cudaStream_t; NULL = legacy
+ *     default stream); no entry point synchronises the host except those
+ *     that say so;
+ *   - return value 0 = success, otherwise a vmc_status code; the message of
+ *     the last failure on the calling thread is vmc_last_error_string().
+ *     No entry point aborts, traps or hangs.
+ */
+#ifndef VMC_GB300_H
+#define VMC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VMC_API_VERSION 1
+
+typedef void* vmc_stream_t;
+
+typedef enum {
+  VMC_OK = 0,
+  VMC_ERR_INVALID_ARGUMENT = 1,
+  VMC_ERR_UNSUPPORTED = 2,
+  VMC_ERR_CUDA = 3,
+  VMC_ERR_TIMEOUT = 4,
+  VMC_ERR_WORKSPACE = 5
+} vmc_status;
+
+/* arithmetic precision of a kernel; parameters are passed in the matching
+ * complex type (VMC_F64: c128, VMC_F32: c64) */
+typedef enum { VMC_F64 = 0, VMC_F32 = 1 } vmc_precision;
+
+/* layouts of per-sample log-derivatives O_k = d log psi / d theta_k */
+typedef enum {
+  /* (N, 2P) c128: per parameter leaf [g, i g] -- the holomorphic flat
+   * gradient of jVMC (vqs.py:66-69, leaf order of get_parameters) */
+  VMC_GRAD_REFERENCE = 0,
+  /* (N, P) c128: one complex derivative per complex parameter */
+  VMC_GRAD_COMPACT = 1
+} vmc_grad_layout;
+
+int vmc_api_version(void);
+const char* vmc_last_error_string(void);
+
+/* ------------------------------------------------------------------------
+ * ExactSampler basis.  Replaces ExactSampler.get_basis /
+ * _get_basis_ldim2 / _get_basis (sampler.py:421-472): state index
+ * first_state + r in row r; for local_dim 2 site i holds bit i of the index,
+ * otherwise the base-local_dim digits most-significant first.
+ * ------------------------------------------------------------------------ */
+int vmc_exact_basis(int32_t* basis, int64_t first_state, int64_t num_states, int32_t num_sites,
+                    int32_t local_dim, vmc_stream_t stream);
+
+/* Born weights of the exact sampler (sampler.py:474-486, 519-524):
+ * p_r = exp((Re log_psi_r - last_norm) / log_prob_factor) for r < num_valid,
+ * else 0; nrm = sum(p); p /= nrm; last_norm += log_prob_factor * log(nrm).
+ * last_norm is a device f64 read and updated in place (ExactSampler.lastNorm);
+ * *norm_out (device f64, optional) receives nrm.
+ * workspace: vmc_reduce_workspace_bytes(1) bytes. */
+int vmc_exact_probabilities(const double* log_psi, int64_t num_states, int64_t num_valid, double* last_norm,
+                            double log_prob_factor, double* p, double* norm_out, void* workspace,
+                            size_t workspace_bytes, vmc_stream_t stream);
+
+/* ------------------------------------------------------------------------
+ * Complex RBM  log psi(s) = sum_j logcosh(sum_i W_ij (2 s_i - 1) + b_j)
+ * (nets/rbm.py:17-38, nets/activation_functions.py:19-22).
+ * kernel: (L, M) row-major, bias: (M) or NULL, in the precision's complex type.
+ * ------------------------------------------------------------------------ */
+
+/* Size in bytes of the per-parameter tables used by the fused local-energy
+ * and Metropolis kernels (4 complex (L, M) tables). */
+size_t vmc_rbm_tables_bytes(int32_t precision, int32_t num_sites, int32_t num_hidden);
+
+/* Fill the tables: cosh(2W), sinh(2W), exp(2W), exp(-2W).  Call after every
+ * parameter change. */
+int vmc_rbm_prepare(int32_t precision, int32_t num_sites, int32_t num_hidden, const void* kernel, void* tables,
+                    vmc_stream_t stream);
+
+/* log psi of num_configs configurations into log_psi (c128).  Replaces
+ * NQS.__call__ / _eval (vqs.py:223-251) for a CpxRBM. */
+int vmc_rbm_logpsi(int32_t precision, const int32_t* configs, int64_t num_configs, int32_t num_sites,
+                   int32_t num_hidden, const void* kernel, const void* bias, double* log_psi, vmc_stream_t stream);
+
+/* Per-sample log-derivatives (holomorphic): d/db_j = tanh(theta_j),
+ * d/dW_ij = (2 s_i - 1) tanh(theta_j).  Replaces NQS.gradients with
+ * flat_gradient_holo (vqs.py:66-69, 256-287).  out is c128 in `layout`. */
+int vmc_rbm_gradients(int32_t precision, const int32_t* configs, int64_t num_configs, int32_t num_sites,
+                      int32_t num_hidden, const void* kernel, const void* bias, int32_t layout, double* out,
+                      vmc_stream_t stream);
+
+/* Metropolis sampling of |psi|^mu with single spin flips.  Replaces
+ * MCSampler._get_samples_mcmc / _get_samples / _sweep with propose_spin_flip
+ * (sampler.py:15-19, 264-358).  One warp per chain; states (num_chains, L)
+ * are read and written back (the chains persist between calls);
+ * therm_steps proposals, then samples_per_chain times sweep_steps proposals
+ * followed by a record, into configs_out (samples_per_chain*num_chains, L)
+ * with row = sample*num_chains + chain (sampler.py:320-323).
+ * Random numbers: Philox4x32-10 with key = seed, counter =
+ * (step, chain, call_index, 0x5EED); site = (r0 * L) >> 32, accept iff
+ * u < |psi(s')/psi(s)|^mu with u = ((r1>>5) 2^26 + (r2>>6)) / 2^53.
+ * counters (device uint64[2]) += {proposed, accepted}.  Needs the tables of
+ * vmc_rbm_prepare. */
+int vmc_rbm_metropolis(int32_t precision, int32_t* states, int32_t num_chains, int32_t num_sites,
+                       int32_t num_hidden, const void* kernel, const void* bias, const void* tables, double mu,
+                       uint64_t seed, uint32_t call_index, int64_t therm_steps, int64_t sweep_steps,
+                       int64_t samples_per_chain, int32_t* configs_out, void* counters, vmc_stream_t stream);
+
+/* Host-side copy of the Metropolis random stream (no GPU needed): flip sites
+ * and acceptance uniforms of `step` for chains 0..num_chains-1 (host arrays). */
+int vmc_metropolis_draws_host(uint64_t seed, uint32_t call_index, uint32_t step, int32_t num_chains,
+                              int32_t num_sites, int32_t* sites, double* uniforms);
+
+/* Metropolis weights p_r = exp(factor * Re log_psi_r) / sum (sampler.py:234-235,
+ * factor = 1/logProbFactor - mu).  workspace: vmc_reduce_workspace_bytes(1). */
+int vmc_mc_probabilities(const double* log_psi, int64_t num_samples, double factor, double* p, void* workspace,
+                         size_t workspace_bytes, vmc_stream_t stream);
+
+/* ------------------------------------------------------------------------
+ * Branch-free operators (operator/branch_free.py:311-487).
+ * The tables are those of BranchFreeOperator.compile (348-414): every
+ * operator string is stored right-to-left and padded with Id(0).
+ * ------------------------------------------------------------------------ */
+typedef struct {
+  int32_t num_ops;       /* number of operator strings                      */
+  int32_t max_len;       /* maxOpStrLength                                  */
+  int32_t local_dim;     /* lDim                                             */
+  int32_t num_diag;      /* number of diagonal strings                       */
+  const int32_t* idx;    /* (num_ops, max_len) site index                    */
+  const int32_t* map;    /* (num_ops, max_len, local_dim) new local state    */
+  const double* mat_els; /* (num_ops, max_len, local_dim) c128               */
+  const int32_t* fermi;  /* (num_ops, max_len) 1 = fermionic operator        */
+  const double* prefactor; /* (num_ops) c128, arg_fun(*args) (416-438)      */
+  const int32_t* diag;   /* (num_diag) indices of the diagonal strings       */
+} vmc_bf_operator;
+
+/* Maximum operator-string length the kernels accept. */
+#define VMC_BF_MAX_LEN 16
+
+/* Matrix elements of every string for every configuration, the diagonal
+ * merge (branch_free.py:483-485) and the nonzero compaction of
+ * Operator._find_nonzero (base.py:91-103): mat_el_full (N, num_ops) c128,
+ * nz_index (N, num_ops) ascending indices of |m| > 1e-6, nz_count (N),
+ * *max_count (device int32) = max nz_count (the value of
+ * jnp.max(numNonzero) in base.py:157). */
+int vmc_bf_matrix_elements(const int32_t* configs, int64_t num_configs, int32_t num_sites,
+                           const vmc_bf_operator* op, double* mat_el_full, int32_t* nz_index, int32_t* nz_count,
+                           int32_t* max_count, vmc_stream_t stream);
+
+/* s' and matrix elements in the reference layout of Operator.get_s_primes
+ * (base.py:116-160): s_primes (N*K, L) and mat_el (N, K) c128; entries past
+ * nz_count are the last string's s' with matrix element 0
+ * (set_zero_to_zero, base.py:105-114).  K = the max_count above. */
+int vmc_bf_gather(const int32_t* configs, int64_t num_configs, int32_t num_sites, const vmc_bf_operator* op,
+                  const double* mat_el_full, const int32_t* nz_index, const int32_t* nz_count, int32_t K,
+                  int32_t* s_primes, double* mat_el, vmc_stream_t stream);
+
+/* O_loc(s) = sum_k mat_el_k exp(log psi(s'_k) - log psi(s))
+ * (Operator._get_O_loc, base.py:162-164). */
+int vmc_oloc_from_sprimes(const double* mat_el, const double* log_psi_s, const double* log_psi_sp,
+                          int64_t num_configs, int32_t K, double* oloc, vmc_stream_t stream);
+
+/* Fused local estimator for a CpxRBM: O_loc(s) of a branch-free operator
+ * without materialising s' (replaces get_s_primes + psi(s') + _get_O_loc,
+ * base.py:166-192).  Uses the tables of vmc_rbm_prepare.  local_dim 2.
+ * log_psi_s (c128, optional): the caller's log psi(s); when given the result
+ * is sum_k m_k exp(log psi(s'_k) - log_psi_s) exactly as base.py:162-164,
+ * when NULL the network's own log psi(s) is used. */
+int vmc_rbm_oloc_fused(int32_t precision, const int32_t* configs, int64_t num_configs, int32_t num_sites,
+                       int32_t num_hidden, const void* kernel, const void* bias, const void* tables,
+                       const vmc_bf_operator* op, const double* log_psi_s, double* oloc, vmc_stream_t stream);
+
+/* ------------------------------------------------------------------------
+ * Sample statistics (stats.py:197-265, mpi_wrapper.py:114-217), FP64,
+ * fixed-order (bitwise reproducible) reductions.
+ * ------------------------------------------------------------------------ */
+
+/* Workspace bytes of a reduction producing `num_outputs` c128 values. */
+size_t vmc_reduce_workspace_bytes(int64_t num_outputs);
+
+/* mean = sum_n w_n x_n (c128), var = sum_n w_n |x_n - mean|^2 (f64). */
+int vmc_weighted_mean_var(const double* x, const double* w, int64_t n, double* mean, double* var, void* workspace,
+                          size_t workspace_bytes, vmc_stream_t stream);
+
+/* Mean of the RBM log-derivatives and the force for the compact layout:
+ * ok_mean_k = sum_n w_n O_nk, force_k = sum_n w_n conj(O_nk - ok_mean_k)(E_n - eloc_mean)
+ * (stats.py:50-58 via tdvp.py:139-142), without materialising O.  P = M + L*M
+ * with bias, L*M without.  workspace: vmc_rbm_grad_stats_workspace_bytes. */
+size_t vmc_rbm_grad_stats_workspace_bytes(int64_t num_configs, int32_t num_sites, int32_t num_hidden);
+int vmc_rbm_grad_stats(int32_t precision, const int32_t* configs, int64_t num_configs, int32_t num_sites,
+                       int32_t num_hidden, const void* kernel, const void* bias, const double* weights,
+                       const double* eloc, const double* eloc_mean, double* ok_mean, double* force,
+                       void* workspace, size_t workspace_bytes, vmc_stream_t stream);
+
+/* ------------------------------------------------------------------------
+ * Centred, weighted data of the S/F build and of the SNR transform
+ * (stats.py:197-205, 255-292; tdvp.py:134-181) for a CpxRBM.
+ * ------------------------------------------------------------------------ */
+typedef enum {
+  VMC_DATA_C128 = 0,   /* (N, P) complex128                                   */
+  VMC_DATA_C64 = 1,    /* (N, P) complex64                                    */
+  VMC_DATA_BF16X2 = 2  /* bf16 hi (out) and lo (out_lo) planes of the real
+                        * representation [Re | Im]: (2P, N) for gradients,
+                        * (N, 2P) for SNR data; value ~ hi + lo            */
+} vmc_data_format;
+
+/* X_nk = sqrt(w_n) (O_nk - ok_mean_k), O in the compact layout. */
+int vmc_rbm_centered_gradients(int32_t precision, const int32_t* configs, int64_t num_configs, int32_t num_sites,
+                               int32_t num_hidden, const void* kernel, const void* bias, const double* weights,
+                               const double* ok_mean, int32_t format, void* out, void* out_lo, vmc_stream_t stream);
+
+/* H_nk = sqrt(w_n) ((neg_rhs) (E_n - Ebar) conj(O_nk - ok_mean_k) - force_k): the
+ * per-sample data of covar_data(O, E).transform(makeReal(-x .)) before the
+ * eigenbasis projection (tdvp.py:173-181); neg_rhs = -rhsPrefactor, force =
+ * -rhsPrefactor * covar(O, E). */
+int vmc_rbm_snr_data(int32_t precision, const int32_t* configs, int64_t num_configs, int32_t num_sites,
+                     int32_t num_hidden, const void* kernel, const void* bias, const double* weights,
+                     const double* ok_mean, const double* eloc, const double* eloc_mean, double neg_rhs_re,
+                     double neg_rhs_im, const double* force, int32_t format, void* out, void* out_lo,
+                     vmc_stream_t stream);
+
+/* ------------------------------------------------------------------------
+ * TDVP solve helpers (util/tdvp.py:134-213), complex P-dimensional form.
+ * ------------------------------------------------------------------------ */
+
+/* Hermitian A (P x P, c128, both triangles) from the Gram matrix G of the
+ * real representation [Re X | Im X] (2P x 2P, row-major, leading dimension
+ * ld_gram, only row <= col read) with A_aa *= 1 + diag_shift. */
+int vmc_gram_to_hermitian(int32_t gram_precision, const void* gram, int64_t ld_gram, int32_t num_params,
+                          double diag_shift, double* A, vmc_stream_t stream);
+
+/* y = U^H x (adjoint = 1) or y = U x (adjoint = 0); U column-major c128. */
+int vmc_zgemv(int32_t adjoint, const double* U, int64_t ld, int32_t n, const double* x, double* y,
+              vmc_stream_t stream);
+
+/* The SNR of every eigenvector: snr_k = sqrt(|N |VtF_k|^2 / rhoVar_k|) with
+ * rhoVar_k = colsq[k] (+ colsq[n + k] when real_rep), colsq the column sums of
+ * |projected SNR data|^2 (tdvp.py:173-181). */
+int vmc_tdvp_snr(const double* vtf, int32_t colsq_precision, const void* colsq, int32_t n, int32_t real_rep,
+                 double num_samples, double* snr, double* rho_var, vmc_stream_t stream);
+
+/* The regularised pseudo-inverse cutoff loop (tdvp.py:191-209) on the
+ * device: pinv (n) and result[3] = {residual, cutoff used, iterations}.
+ * snr NULL = exact sampling (no SNR factor). ev ascending. */
+int vmc_tdvp_regularize(const double* ev, const double* vtf, const double* snr, int32_t n, double pinv_cutoff,
+                        double pinv_tol, double snr_tol, double* pinv, double* result, vmc_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VMC_GB300_H */

@@ -1,0 +1,121 @@
+"""C ABI and host logic without a GPU: the library loads, exports every
+symbol the header declares, validates arguments before touching the device,
+and its random stream and operator tables match the oracle's."""
+
+import ctypes
+import glob
+import os
+import re
+
+import numpy as np
+import pytest
+
+import vmc_jax_gb300._lib as L
+from oracle import jvmc_oracle as O
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        src = re.sub(r"/\*.*?\*/", "", open(h).read(), flags=re.S)
+        names |= set(re.findall(r"\b(vmc_\w+)\s*\(", src))
+    return names
+
+
+def test_library_exports_every_declared_symbol():
+    lib = L.load()
+    syms = declared_symbols()
+    assert len(syms) >= 20
+    for s in syms:
+        assert hasattr(lib, s), s
+    assert lib.vmc_api_version() == 1
+
+
+def test_header_prototypes_parse():
+    protos = L.parse_header()
+    assert set(protos) == declared_symbols()
+
+
+def test_invalid_arguments_are_rejected_on_the_host():
+    lib = L.load()
+    rc = lib.vmc_exact_basis(None, 0, 10, 4, 2, None)
+    assert rc == 1
+    assert b"null output" in lib.vmc_last_error_string()
+    rc = lib.vmc_exact_basis(ctypes.c_void_p(16), 0, 10, 70, 2, None)
+    assert rc == 2
+    rc = lib.vmc_rbm_logpsi(7, ctypes.c_void_p(16), 1, 4, 2, ctypes.c_void_p(16), None, ctypes.c_void_p(16), None)
+    assert rc == 2 and b"precision" in lib.vmc_last_error_string()
+    op = L.BfOperator(num_ops=2, max_len=40, local_dim=2, num_diag=0)
+    rc = lib.vmc_bf_matrix_elements(ctypes.c_void_p(16), 1, 4, ctypes.byref(op), None, None, None, None, None)
+    assert rc == 2
+    rc = lib.vmc_rbm_metropolis(0, ctypes.c_void_p(16), 4, 4, 2, ctypes.c_void_p(16), None, ctypes.c_void_p(16),
+                                3.0, 1, 0, 10, 4, 2, ctypes.c_void_p(16), ctypes.c_void_p(16), None)
+    assert rc == 1 and b"mu" in lib.vmc_last_error_string()
+    rc = lib.vmc_weighted_mean_var(ctypes.c_void_p(16), ctypes.c_void_p(16), 10, ctypes.c_void_p(16),
+                                   ctypes.c_void_p(16), ctypes.c_void_p(16), 8, None)
+    assert rc == 5
+
+
+@pytest.mark.parametrize("seed,call,step,L_", [(0, 0, 0, 10), (0x123456789ABCDEF, 3, 17, 64), (7, 9, 12345, 100)])
+def test_philox_stream_matches_oracle(seed, call, step, L_):
+    lib = L.load()
+    C = 777
+    s = np.zeros(C, np.int32)
+    u = np.zeros(C)
+    assert lib.vmc_metropolis_draws_host(seed, call, step, C, L_, s.ctypes.data, u.ctypes.data) == 0
+    s2, u2 = O.metropolis_draws(seed, call, step, C, L_)
+    assert np.array_equal(s, s2) and np.array_equal(u, u2)
+    assert s.min() >= 0 and s.max() < L_ and u.min() >= 0 and u.max() < 1
+
+
+def test_philox_known_answer():
+    """Philox4x32-10 test vector of the Random123 distribution (kat_vectors):
+    counter 0, key 0 -> 6627e8d5 e169c58d bc57ac4c 9b00dbd8."""
+    r = O.philox4x32(0, 0, 0, 0, 0, 0)
+    assert [int(x) for x in r] == [0x6627e8d5, 0xe169c58d, 0xbc57ac4c, 0x9b00dbd8]
+
+
+def test_operator_tables_match_oracle():
+    import vmc_jax_gb300.operator as op
+    H = op.BranchFreeOperator()
+    Ho = O.BranchFreeOperator()
+    L_ = 6
+    for l in range(L_):
+        H.add(op.scal_opstr(-1.0, (op.Sz(l), op.Sz((l + 1) % L_))))
+        H.add(op.scal_opstr(lambda t: 0.3 * t, (op.Sx(l),)))
+        H.add((op.Sy(l), op.Sz((l + 2) % L_), op.Sx((l + 1) % L_)))
+        Ho.add(O.scal_opstr(-1.0, (O.Sz(l), O.Sz((l + 1) % L_))))
+        Ho.add(O.scal_opstr(lambda t: 0.3 * t, (O.Sx(l),)))
+        Ho.add((O.Sy(l), O.Sz((l + 2) % L_), O.Sx((l + 1) % L_)))
+    try:
+        H.compile()
+    except Exception:
+        pass  # uploading needs a GPU; the host tables are built first
+    Ho.compile()
+    assert np.array_equal(H.idxC, Ho.idxC)
+    assert np.array_equal(H.mapC, Ho.mapC)
+    assert np.array_equal(H.matElsC, Ho.matElsC)
+    assert np.array_equal(H.diag, Ho.diag)
+    assert np.allclose(H.arg_fun(2.0), Ho.arg_fun(2.0))
+
+
+def test_opstr_algebra():
+    """tests/operator_test.py:256-265."""
+    import vmc_jax_gb300.operator as op
+    op1 = op.Sz(3)
+    op2 = op.Sx(5)
+    opstr1 = 13. * op1 * op2
+    opstr2 = 1.j * opstr1 * op1
+    assert np.allclose(opstr2[0](), 13.j)
+    for o in opstr2[1:]:
+        assert isinstance(o, (op.LocalOp, dict))
+
+
+def test_distribute_sampling():
+    import vmc_jax_gb300.mpi_wrapper as mpi
+    assert mpi.distribute_sampling(16384, localDevices=1, numChainsPerDevice=1024) == (16, 16384)
+    assert mpi.distribute_sampling(1000, localDevices=1, numChainsPerDevice=777) == (2, 1554)
+    assert mpi.distribute_sampling(1024) == (1024, 1024)
+    assert mpi.globNumSamples == 1024

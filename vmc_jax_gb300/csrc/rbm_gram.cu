@@ -1,0 +1,229 @@
+// Producers of the centred, weighted log-derivative data that the S/F build
+// and the SNR transform contract (stats.py:197-205, 255-292 via
+// tdvp.py:134-181), for a CpxRBM, in three storage formats:
+//   VMC_DATA_C128   (N, P) complex128
+//   VMC_DATA_C64    (N, P) complex64
+//   VMC_DATA_BF16X2 bf16 hi/lo planes of the real representation
+//                   [Re X | Im X]: transposed (2P, N) for the Gram operand
+//                   (sample index contiguous), row-major (N, 2P) for the
+//                   SNR operand.
+// X_nk = sqrt(w_n) (O_nk - mean_k)            (gradients)
+// H_nk = sqrt(w_n) (-x dE_n conj(O_nk - mean_k) - f_k)   (SNR data; dE_n = E_n - Ebar)
+#include <cuda_bf16.h>
+
+#include <algorithm>
+
+#include "vmc_common.cuh"
+
+namespace vmc {
+
+
+// tanh(theta) of kTileN samples into shared memory (as T), one warp per sample.
+template <typename T>
+__device__ void tile_tanh(const int32_t* __restrict__ configs, int64_t n0, int64_t N, int L, int M,
+                          const cpx<T>* __restrict__ W, const cpx<T>* __restrict__ b, cpx<T>* tt, int8_t* sg,
+                          int kTileN) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+  for (int r = warp; r < kTileN; r += nwarps) {
+    const int64_t n = n0 + r;
+    int8_t* cfg = sg + r * L;
+    if (n < N) {
+      for (int i = lane; i < L; i += 32) cfg[i] = (int8_t)configs[n * L + i];
+    } else {
+      for (int i = lane; i < L; i += 32) cfg[i] = 0;
+    }
+    __syncwarp();
+    for (int j = lane; j < M; j += 32) {
+      cpx<T> th = b ? b[j] : mk(T(0), T(0));
+      for (int i = 0; i < L; ++i) {
+        cpx<T> x = W[(size_t)i * M + j];
+        if (cfg[i]) {
+          th.re += x.re;
+          th.im += x.im;
+        } else {
+          th.re -= x.re;
+          th.im -= x.im;
+        }
+      }
+      tt[(size_t)r * M + j] = n < N ? ctanh_(th) : mk(T(0), T(0));
+    }
+  }
+  __syncthreads();
+}
+
+struct data_args {
+  int64_t N;
+  int L, M;
+  bool hasBias;
+  const double* w;         // (N) weights
+  const double2* okMean;   // (P) c128
+  const double2* eloc;     // (N) c128 or null (gradients)
+  const double2* elocMean; // (1) c128
+  double2 xfac;            // -x (rhs prefactor, negated)
+  const double2* force;    // (P) f_k = -x * covar(O,E)_k (SNR data) or null
+  int format;
+  int tileN;  // samples per block
+  void* out;
+  void* out2;              // lo plane for BF16X2
+};
+
+// value of column k (complex) for tile row r
+template <typename T>
+__device__ __forceinline__ cpx<double> data_value(const data_args& a, const cpx<T>* tt, const int8_t* sg, int r,
+                                                  int64_t n, int k, double sw) {
+  const int P0 = a.hasBias ? a.M : 0;
+  cpx<T> o;
+  if (k < P0) {
+    o = tt[(size_t)r * a.M + k];
+  } else {
+    const int kk = k - P0;
+    const int i = kk / a.M, j = kk - (kk / a.M) * a.M;
+    cpx<T> t = tt[(size_t)r * a.M + j];
+    o = sg[r * a.L + i] ? t : mk(-t.re, -t.im);
+  }
+  const double2 mu = a.okMean[k];
+  cpx<double> d = mk((double)o.re - mu.x, (double)o.im - mu.y);
+  if (a.eloc) {
+    const double2 e = a.eloc[n], em = *a.elocMean;
+    cpx<double> de = mk(e.x - em.x, e.y - em.y);
+    cpx<double> h = mk(a.xfac.x, a.xfac.y) * (de * conjg(d));
+    const double2 f = a.force[k];
+    d = mk(h.re - f.x, h.im - f.y);
+  }
+  return mk(sw * d.re, sw * d.im);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) rbm_data_kernel(const int32_t* __restrict__ configs, const cpx<T>* __restrict__ W,
+                                                       const cpx<T>* __restrict__ b, data_args a) {
+  extern __shared__ unsigned char smem[];
+  const int kTileN = a.tileN;
+  cpx<T>* tt = reinterpret_cast<cpx<T>*>(smem);
+  int8_t* sg = reinterpret_cast<int8_t*>(smem + (size_t)kTileN * a.M * sizeof(cpx<T>));
+  const int64_t n0 = (int64_t)blockIdx.x * kTileN;
+  tile_tanh<T>(configs, n0, a.N, a.L, a.M, W, b, tt, sg, kTileN);
+  const int P = a.M * a.L + (a.hasBias ? a.M : 0);
+  const int tid = threadIdx.x;
+  if (a.format == VMC_DATA_BF16X2 && a.eloc == nullptr) {
+    // transposed planes (2P, N): thread -> (sample lane r, column group)
+    __nv_bfloat16* hi = reinterpret_cast<__nv_bfloat16*>(a.out);
+    __nv_bfloat16* lo = reinterpret_cast<__nv_bfloat16*>(a.out2);
+    const int r = tid % kTileN;
+    const int cg = tid / kTileN, ncg = blockDim.x / kTileN;
+    const int64_t n = n0 + r;
+    if (n < a.N) {
+      const double sw = sqrt(a.w[n]);
+      for (int k = cg; k < P; k += ncg) {
+        cpx<double> v = data_value<T>(a, tt, sg, r, n, k, sw);
+        float vr = (float)v.re, vi = (float)v.im;
+        __nv_bfloat16 hr = __float2bfloat16_rn(vr), hi_ = __float2bfloat16_rn(vi);
+        hi[(size_t)k * a.N + n] = hr;
+        lo[(size_t)k * a.N + n] = __float2bfloat16_rn(vr - __bfloat162float(hr));
+        hi[(size_t)(P + k) * a.N + n] = hi_;
+        lo[(size_t)(P + k) * a.N + n] = __float2bfloat16_rn(vi - __bfloat162float(hi_));
+      }
+    }
+    return;
+  }
+  // row-major formats: thread -> column, loop over the tile's samples
+  for (int r = 0; r < kTileN; ++r) {
+    const int64_t n = n0 + r;
+    if (n >= a.N) break;
+    const double sw = sqrt(a.w[n]);
+    for (int k = tid; k < P; k += blockDim.x) {
+      cpx<double> v = data_value<T>(a, tt, sg, r, n, k, sw);
+      if (a.format == VMC_DATA_C128) {
+        reinterpret_cast<double2*>(a.out)[n * P + k] = make_double2(v.re, v.im);
+      } else if (a.format == VMC_DATA_C64) {
+        reinterpret_cast<float2*>(a.out)[n * P + k] = make_float2((float)v.re, (float)v.im);
+      } else {  // BF16X2 row-major (N, 2P)
+        __nv_bfloat16* hi = reinterpret_cast<__nv_bfloat16*>(a.out);
+        __nv_bfloat16* lo = reinterpret_cast<__nv_bfloat16*>(a.out2);
+        float vr = (float)v.re, vi = (float)v.im;
+        __nv_bfloat16 hr = __float2bfloat16_rn(vr), hi_ = __float2bfloat16_rn(vi);
+        hi[n * 2 * P + k] = hr;
+        lo[n * 2 * P + k] = __float2bfloat16_rn(vr - __bfloat162float(hr));
+        hi[n * 2 * P + P + k] = hi_;
+        lo[n * 2 * P + P + k] = __float2bfloat16_rn(vi - __bfloat162float(hi_));
+      }
+    }
+  }
+}
+
+}  // namespace vmc
+
+using namespace vmc;
+
+static int launch_data(int32_t precision, const int32_t* configs, const void* kernel, const void* bias, data_args a,
+                       vmc_stream_t stream, const char* fn) {
+  VMC_REQUIRE(precision == VMC_F64 || precision == VMC_F32, VMC_ERR_UNSUPPORTED, "%s: precision %d", fn, precision);
+  VMC_REQUIRE(a.format == VMC_DATA_C128 || a.format == VMC_DATA_C64 || a.format == VMC_DATA_BF16X2,
+              VMC_ERR_INVALID_ARGUMENT, "%s: unknown format %d", fn, a.format);
+  VMC_REQUIRE(a.out && (a.format != VMC_DATA_BF16X2 || a.out2), VMC_ERR_INVALID_ARGUMENT, "%s: null output", fn);
+  VMC_REQUIRE(a.N > 0 && a.L > 0 && a.M > 0 && configs && kernel && a.w && a.okMean, VMC_ERR_INVALID_ARGUMENT,
+              "%s: bad arguments", fn);
+  const size_t el = precision == VMC_F64 ? 16 : 8;
+  int kTileN = 64;
+  while (kTileN > 8 && (size_t)kTileN * (a.M * el + a.L) > 200 * 1024) kTileN /= 2;
+  a.tileN = kTileN;
+  const size_t smem = (size_t)kTileN * a.M * el + (size_t)kTileN * a.L;
+  VMC_REQUIRE(smem <= 227 * 1024, VMC_ERR_UNSUPPORTED, "%s: M=%d, L=%d too large for one tile", fn, a.M, a.L);
+  const int grid = (int)((a.N + kTileN - 1) / kTileN);
+  cudaStream_t st = as_stream(stream);
+  if (precision == VMC_F64) {
+    if (smem > 48 * 1024)
+      cudaFuncSetAttribute((const void*)rbm_data_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    rbm_data_kernel<double><<<grid, 256, smem, st>>>(configs, reinterpret_cast<const cpx<double>*>(kernel),
+                                                    reinterpret_cast<const cpx<double>*>(bias), a);
+  } else {
+    if (smem > 48 * 1024)
+      cudaFuncSetAttribute((const void*)rbm_data_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    rbm_data_kernel<float><<<grid, 256, smem, st>>>(configs, reinterpret_cast<const cpx<float>*>(kernel),
+                                                   reinterpret_cast<const cpx<float>*>(bias), a);
+  }
+  return check_launch(fn);
+}
+
+extern "C" int vmc_rbm_centered_gradients(int32_t precision, const int32_t* configs, int64_t num_configs,
+                                          int32_t num_sites, int32_t num_hidden, const void* kernel, const void* bias,
+                                          const double* weights, const double* ok_mean, int32_t format, void* out,
+                                          void* out_lo, vmc_stream_t stream) {
+  data_args a;
+  a.N = num_configs;
+  a.L = num_sites;
+  a.M = num_hidden;
+  a.hasBias = bias != nullptr;
+  a.w = weights;
+  a.okMean = reinterpret_cast<const double2*>(ok_mean);
+  a.eloc = nullptr;
+  a.elocMean = nullptr;
+  a.xfac = make_double2(0, 0);
+  a.force = nullptr;
+  a.format = format;
+  a.out = out;
+  a.out2 = out_lo;
+  return launch_data(precision, configs, kernel, bias, a, stream, "vmc_rbm_centered_gradients");
+}
+
+extern "C" int vmc_rbm_snr_data(int32_t precision, const int32_t* configs, int64_t num_configs, int32_t num_sites,
+                                int32_t num_hidden, const void* kernel, const void* bias, const double* weights,
+                                const double* ok_mean, const double* eloc, const double* eloc_mean,
+                                double neg_rhs_re, double neg_rhs_im, const double* force, int32_t format, void* out,
+                                void* out_lo, vmc_stream_t stream) {
+  VMC_REQUIRE(eloc && eloc_mean && force, VMC_ERR_INVALID_ARGUMENT, "vmc_rbm_snr_data: null argument");
+  data_args a;
+  a.N = num_configs;
+  a.L = num_sites;
+  a.M = num_hidden;
+  a.hasBias = bias != nullptr;
+  a.w = weights;
+  a.okMean = reinterpret_cast<const double2*>(ok_mean);
+  a.eloc = reinterpret_cast<const double2*>(eloc);
+  a.elocMean = reinterpret_cast<const double2*>(eloc_mean);
+  a.xfac = make_double2(neg_rhs_re, neg_rhs_im);
+  a.force = reinterpret_cast<const double2*>(force);
+  a.format = format;
+  a.out = out;
+  a.out2 = out_lo;
+  return launch_data(precision, configs, kernel, bias, a, stream, "vmc_rbm_snr_data");
+}

@@ -1,0 +1,192 @@
+// FP64 pieces of the SNR-regularised TDVP solve (util/tdvp.py:134-213),
+// in the complex P-dimensional form of a holomorphic ansatz (the reference's
+// 2P real representation has the same eigenvalues, each paired, and the
+// same solution; see vmc_tdvp_regularize).
+#include <algorithm>
+
+#include "reduce.cuh"
+#include "vmc_common.cuh"
+
+namespace vmc {
+
+// A[a][b] = (G[a][b] + G[P+a][P+b]) + i (G[a][P+b] - G[b][P+a]) from the Gram
+// matrix G = R^T R of the real representation R = [Re X | Im X], reading only
+// entries with row <= col (upper tiles), with A[b][a] = conj(A[a][b]) and
+// the diagonal shift A[a][a] *= 1 + shift (tdvp.py:144-145).
+template <typename T>
+__global__ void gram_to_hermitian_kernel(const T* __restrict__ G, int64_t ldg, int P, double shift,
+                                         double2* __restrict__ A) {
+  const int64_t total = (int64_t)P * P;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int a = (int)(t / P), b = (int)(t - (t / P) * P);
+    const int r = a <= b ? a : b, c = a <= b ? b : a;  // r <= c
+    double re = (double)G[(int64_t)r * ldg + c] + (double)G[(int64_t)(P + r) * ldg + (P + c)];
+    double im = (double)G[(int64_t)r * ldg + (P + c)] - (double)G[(int64_t)c * ldg + (P + r)];
+    if (a > b) im = -im;
+    if (a == b) {
+      im = 0.0;
+      re *= (1.0 + shift);
+    }
+    A[t] = make_double2(re, im);
+  }
+}
+
+// y_k = sum_j conj(U_jk) x_j ; U column-major (U_jk at k*ld + j): warp per k.
+__global__ void gemv_adjoint_kernel(const double2* __restrict__ U, int64_t ld, int n, const double2* __restrict__ x,
+                                    double2* __restrict__ y) {
+  const int lane = threadIdx.x & 31;
+  const int64_t wid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t k = wid; k < n; k += nw) {
+    const double2* col = U + k * ld;
+    double re = 0.0, im = 0.0;
+    for (int j = lane; j < n; j += 32) {
+      double2 u = col[j], v = x[j];
+      re += u.x * v.x + u.y * v.y;
+      im += u.x * v.y - u.y * v.x;
+    }
+    re = warp_sum(re);
+    im = warp_sum(im);
+    if (lane == 0) y[k] = make_double2(re, im);
+  }
+}
+
+// y_j = sum_k U_jk x_k ; U column-major: thread per j, k loop (coalesced over j).
+__global__ void gemv_kernel(const double2* __restrict__ U, int64_t ld, int n, const double2* __restrict__ x,
+                            double2* __restrict__ y) {
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
+    double re = 0.0, im = 0.0;
+    for (int k = 0; k < n; ++k) {
+      double2 u = U[(int64_t)k * ld + j], v = x[k];
+      re += u.x * v.x - u.y * v.y;
+      im += u.x * v.y + u.y * v.x;
+    }
+    y[j] = make_double2(re, im);
+  }
+}
+
+// The cutoff loop of TDVP.solve (tdvp.py:191-213) on the device, one block.
+// Eigen-pairs (ev_k, u_k) of the complex P x P matrix A stand for the 2P
+// real-representation pairs of the reference: the two members of a pair
+// share |ev/ev_max|, the SNR and |pinv*ev - 1|, and together carry |u^H f|^2
+// of the reference's |V^T F|^2, so the residual sums over k are identical.
+//   invEv = 1/ev where |ev/ev_max| > 1e-14 else 0
+//   cutoff = 1e-2; while residual > pinvTol and cutoff > pinvCutoff:
+//     cutoff *= 0.8; reg = 1/(1 + (max(cutoff,pinvCutoff)/|ev/ev_max|)^6) [* 1/(1+(snrTol/snr)^6)]
+//     pinvEv = invEv * reg; residual = ||(pinvEv ev - 1) VtF|| / ||F||
+// out: pinv (n), result[0] = residual, result[1] = max(cutoff, pinvCutoff).
+__global__ void tdvp_regularize_kernel(const double* __restrict__ ev, const double2* __restrict__ vtf,
+                                       const double* __restrict__ snr, int n, double pinvCutoff,
+                                       double pinvTol, double snrTol, double* __restrict__ pinv,
+                                       double* __restrict__ result, int maxIter) {
+  double fn = 0.0;
+  for (int k = threadIdx.x; k < n; k += blockDim.x) fn += abs2(mk(vtf[k].x, vtf[k].y));
+  // ||F||^2 = sum_k |u_k^H f|^2 (U unitary)
+  fn = block_sum(fn);
+  const double Fnorm = sqrt(fn);
+  const double evMax = ev[n - 1];  // ev ascending: ev[-1] of the reference
+  double residual = 1.0, cutoff = 1e-2;
+  int it = 0;
+  while (residual > pinvTol && cutoff > pinvCutoff && it < maxIter) {
+    ++it;
+    cutoff *= 0.8;
+    const double c = cutoff > pinvCutoff ? cutoff : pinvCutoff;
+    double acc = 0.0;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+      const double e = ev[k];
+      const double rel = fabs(e / evMax);
+      const double inv = rel > 1e-14 ? 1.0 / e : 0.0;
+      const double q = c / rel;
+      const double q2 = q * q;
+      double reg = 1.0 / (1.0 + q2 * q2 * q2);
+      if (snr) {
+        const double s = snrTol / snr[k];
+        const double s2 = s * s;
+        reg *= 1.0 / (1.0 + s2 * s2 * s2);
+      }
+      const double pv = inv * reg;
+      pinv[k] = pv;
+      const double d = pv * e - 1.0;
+      acc += d * d * abs2(mk(vtf[k].x, vtf[k].y));
+    }
+    acc = block_sum(acc);
+    residual = sqrt(acc) / Fnorm;
+  }
+  if (threadIdx.x == 0) {
+    result[0] = residual;
+    result[1] = cutoff > pinvCutoff ? cutoff : pinvCutoff;
+    result[2] = (double)it;
+  }
+}
+
+// snr_k = sqrt(|N |VtF_k|^2 / rhoVar_k|) with rhoVar_k = colsq[k] + colsq[P+k]
+// (the two real components of the complex projection, tdvp.py:173-181).
+template <typename T>
+__global__ void snr_kernel(const double2* __restrict__ vtf, const T* __restrict__ colsq, int n, int realRep,
+                           double numSamples, double* __restrict__ snr, double* __restrict__ rhoVar) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    double rv = realRep ? (double)colsq[k] + (double)colsq[n + k] : (double)colsq[k];
+    if (rhoVar) rhoVar[k] = rv;
+    snr[k] = sqrt(fabs(numSamples * abs2(mk(vtf[k].x, vtf[k].y)) / rv));
+  }
+}
+
+}  // namespace vmc
+
+using namespace vmc;
+
+extern "C" int vmc_gram_to_hermitian(int32_t gram_precision, const void* gram, int64_t ld_gram, int32_t num_params,
+                                     double diag_shift, double* A, vmc_stream_t stream) {
+  VMC_REQUIRE(gram && A && num_params > 0 && ld_gram >= 2 * (int64_t)num_params, VMC_ERR_INVALID_ARGUMENT,
+              "vmc_gram_to_hermitian: bad arguments");
+  int64_t total = (int64_t)num_params * num_params;
+  int blocks = (int)std::min<int64_t>((total + 255) / 256, 152 * 32);
+  if (gram_precision == VMC_F64)
+    gram_to_hermitian_kernel<double><<<blocks, 256, 0, as_stream(stream)>>>(
+        reinterpret_cast<const double*>(gram), ld_gram, num_params, diag_shift, reinterpret_cast<double2*>(A));
+  else
+    gram_to_hermitian_kernel<float><<<blocks, 256, 0, as_stream(stream)>>>(
+        reinterpret_cast<const float*>(gram), ld_gram, num_params, diag_shift, reinterpret_cast<double2*>(A));
+  return check_launch("vmc_gram_to_hermitian");
+}
+
+extern "C" int vmc_zgemv(int32_t adjoint, const double* U, int64_t ld, int32_t n, const double* x, double* y,
+                         vmc_stream_t stream) {
+  VMC_REQUIRE(U && x && y && n > 0 && ld >= n, VMC_ERR_INVALID_ARGUMENT, "vmc_zgemv: bad arguments");
+  if (adjoint) {
+    int blocks = (int)std::min<int64_t>(((int64_t)n * 32 + 255) / 256, 152 * 16);
+    gemv_adjoint_kernel<<<blocks, 256, 0, as_stream(stream)>>>(reinterpret_cast<const double2*>(U), ld, n,
+                                                               reinterpret_cast<const double2*>(x),
+                                                               reinterpret_cast<double2*>(y));
+  } else {
+    int blocks = (int)std::min<int64_t>(((int64_t)n + 127) / 128, 152 * 16);
+    gemv_kernel<<<blocks, 128, 0, as_stream(stream)>>>(reinterpret_cast<const double2*>(U), ld, n,
+                                                       reinterpret_cast<const double2*>(x),
+                                                       reinterpret_cast<double2*>(y));
+  }
+  return check_launch("vmc_zgemv");
+}
+
+extern "C" int vmc_tdvp_regularize(const double* ev, const double* vtf, const double* snr, int32_t n,
+                                   double pinv_cutoff, double pinv_tol, double snr_tol, double* pinv, double* result,
+                                   vmc_stream_t stream) {
+  VMC_REQUIRE(ev && vtf && pinv && result && n > 0, VMC_ERR_INVALID_ARGUMENT, "vmc_tdvp_regularize: bad arguments");
+  tdvp_regularize_kernel<<<1, 1024, 0, as_stream(stream)>>>(ev, reinterpret_cast<const double2*>(vtf), snr, n,
+                                                          pinv_cutoff, pinv_tol, snr_tol, pinv, result, 100000);
+  return check_launch("vmc_tdvp_regularize");
+}
+
+extern "C" int vmc_tdvp_snr(const double* vtf, int32_t colsq_precision, const void* colsq, int32_t n,
+                            int32_t real_rep, double num_samples, double* snr, double* rho_var, vmc_stream_t stream) {
+  VMC_REQUIRE(vtf && colsq && snr && n > 0, VMC_ERR_INVALID_ARGUMENT, "vmc_tdvp_snr: bad arguments");
+  int blocks = (n + 255) / 256;
+  if (colsq_precision == VMC_F64)
+    snr_kernel<double><<<blocks, 256, 0, as_stream(stream)>>>(reinterpret_cast<const double2*>(vtf),
+                                                              reinterpret_cast<const double*>(colsq), n, real_rep,
+                                                              num_samples, snr, rho_var);
+  else
+    snr_kernel<float><<<blocks, 256, 0, as_stream(stream)>>>(reinterpret_cast<const double2*>(vtf),
+                                                             reinterpret_cast<const float*>(colsq), n, real_rep,
+                                                             num_samples, snr, rho_var);
+  return check_launch("vmc_tdvp_snr");
+}

@@ -1,0 +1,7 @@
+"""Solvers, integrators and drivers (mirror of jVMC.util)."""
+
+from .tdvp import TDVP, realFun, imagFun
+from . import stepper
+from .util import measure, ground_state_search
+
+__all__ = ["TDVP", "realFun", "imagFun", "stepper", "measure", "ground_state_search"]

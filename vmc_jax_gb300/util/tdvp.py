@@ -1,0 +1,375 @@
+"""TDVP solver (mirror of jVMC/util/tdvp.py:26-326).
+
+For a CpxRBM state the right-hand side runs as one GPU pipeline:
+
+  sample -> fused O_loc -> FP64 mean/variance of E_loc -> FP64 means of O_k
+  and force F -> centred data -> Gram contraction S (FP64 / FP32 / mixed
+  BF16x3 on tcgen05) -> FP64 eigendecomposition -> SNR contraction ->
+  cutoff loop on the device -> update.
+
+The holomorphic ansatz makes the reference's 2P real representation of S
+(tdvp.py:144: makeReal of the 2P x 2P covariance) the real representation
+of the complex P x P matrix A = <O^dagger O>_c; its spectrum is that of A
+with every eigenvalue paired ({l, l} for makeReal='real', {l, -l} for
+'imag'), and the update solves A z = -x covar(O, E) with the same
+regulariser, returned as [Re z; Im z] per leaf.  The eigendecomposition is
+therefore done on the P x P complex matrix (cuSOLVER, FP64).
+
+SNR: for makeReal='imag' the SNR of a pair is unique and identical to the
+reference's; for makeReal='real' the reference's eigenvectors within a
+degenerate pair are an arbitrary LAPACK basis and so is the split of the
+SNR between them; here both members get the rotation-invariant pair value
+N|u^H f|^2 / sum_n w_n |u^H (h_n - f)|^2.
+"""
+
+import warnings
+
+import numpy as np
+import torch
+
+from .. import _lib
+from .. import global_defs
+from .. import mpi_wrapper as mpi
+from ..sampler import ExactSampler
+from ..stats import SampledObs
+
+
+def realFun(x):
+    """tdvp.py:14-15."""
+    return torch.real(x) if isinstance(x, torch.Tensor) else np.real(x)
+
+
+def imagFun(x):
+    """tdvp.py:18-19."""
+    return 0.5 * (x - (torch.conj(x) if isinstance(x, torch.Tensor) else np.conj(x)))
+
+
+def transform_helper(x, rhsPrefactor, makeReal):
+    """tdvp.py:22-23."""
+    return makeReal((-rhsPrefactor) * x)
+
+
+class TDVP:
+    """Solver of the TDVP equation  q[S] theta_dot = -q[x F]  by regularised
+    pseudo-inverse (tdvp.py:26-94).
+
+    Initializer arguments as in the reference: ``sampler``, ``snrTol``,
+    ``pinvTol``, ``pinvCutoff``, ``makeReal``, ``rhsPrefactor``,
+    ``diagonalShift``, ``crossValidation``, ``diagonalizeOnDevice`` (must be
+    True: there is no host path).  Additional:
+
+        * ``precision``: arithmetic of the sampling, E_loc and S/F stages:
+          ``"fp64"`` (the reference's), ``"fp32"`` (plain FP32 GPU form:
+          FP32 kernels, FP32 complex GEMMs) or ``"mixed"`` (FP32 kernels,
+          S and the SNR contraction in BF16 with hi/lo split correction and
+          FP32 accumulation on tcgen05).  Means, variances and the
+          eigendecomposition / solve are FP64 in every mode.
+    """
+
+    def __init__(self, sampler, snrTol=2, pinvTol=1e-14, pinvCutoff=1e-8, makeReal='imag', rhsPrefactor=1.j,
+                 diagonalShift=0., crossValidation=False, diagonalizeOnDevice=True, precision="fp64"):
+        if not diagonalizeOnDevice:
+            raise NotImplementedError("diagonalisation runs on the GPU; there is no host path")
+        if precision not in ("fp64", "fp32", "mixed"):
+            raise ValueError("precision must be 'fp64', 'fp32' or 'mixed'")
+        self.sampler = sampler
+        self.snrTol = snrTol
+        self.pinvTol = pinvTol
+        self.pinvCutoff = pinvCutoff
+        self.diagonalShift = diagonalShift
+        self.rhsPrefactor = rhsPrefactor
+        self.crossValidation = crossValidation
+        self.diagonalizeOnDevice = True
+        self.precision = precision
+        self.metaData = None
+        self.makeRealName = makeReal
+        self.makeReal = imagFun if makeReal == 'imag' else realFun
+        self.timings = {}
+
+    def set_diagonal_shift(self, delta):
+        self.diagonalShift = delta
+
+    def set_cross_validation(self, crossValidation=True):
+        self.crossValidation = crossValidation
+
+    def get_residuals(self):
+        return self.metaData["tdvp_error"], self.metaData["tdvp_residual"]
+
+    def get_snr(self):
+        return self.metaData["SNR"]
+
+    def get_spectrum(self):
+        return self.metaData["spectrum"]
+
+    def get_metadata(self):
+        return self.metaData
+
+    def get_energy_variance(self):
+        return self.ElocVar0
+
+    def get_energy_mean(self):
+        return torch.real(self.ElocMean0) if isinstance(self.ElocMean0, torch.Tensor) else np.real(self.ElocMean0)
+
+    def get_S(self):
+        return self.S
+
+    # ================================================= fused CpxRBM path
+    def _rbm_capable(self, psi, hamiltonian):
+        from ..nets.rbm import CpxRBM
+        return isinstance(psi.net, CpxRBM) and hasattr(hamiltonian, "fused_capable") and \
+            hamiltonian.fused_capable(psi)
+
+    def _kernel_precision(self):
+        return "fp64" if self.precision == "fp64" else "fp32"
+
+    def _rbm_rhs(self, psi, configs, Eloc, p, weights=None):
+        """Everything after E_loc for a CpxRBM; returns the 2P update, the
+        residual and the cutoff (device scalars)."""
+        dev = configs.device
+        st = _lib.stream()
+        flat = configs.reshape(configs.shape[0] * configs.shape[1], -1)
+        N, L = flat.shape
+        w = (p if weights is None else weights).reshape(-1).to(torch.float64).contiguous()
+        E = Eloc.reshape(-1).to(torch.complex128).contiguous()
+        kp = self._kernel_precision()
+        params = psi.params_for(kp)
+        prec = psi.net._prec(kp)
+        M = int(params["kernel"].shape[1])
+        hasBias = "bias" in params
+        P = L * M + (M if hasBias else 0)
+        Wk, bk = _lib.ptr(params["kernel"]), _lib.ptr(params.get("bias"))
+
+        # E_loc statistics (stats.py:197-205, 248-252)
+        emean = torch.empty(1, dtype=torch.complex128, device=dev)
+        evar = torch.empty(1, dtype=torch.float64, device=dev)
+        ws = _lib.Workspace.get(_lib.query("vmc_reduce_workspace_bytes", 2))
+        _lib.call("vmc_weighted_mean_var", _lib.ptr(E), _lib.ptr(w), N, _lib.ptr(emean), _lib.ptr(evar),
+                  _lib.ptr(ws), ws.numel(), st)
+        # mean of O_k and covar(O, E) (stats.py:50-58 via tdvp.py:139)
+        okMean = torch.empty(P, dtype=torch.complex128, device=dev)
+        covOE = torch.empty(P, dtype=torch.complex128, device=dev)
+        ws = _lib.Workspace.get(_lib.query("vmc_rbm_grad_stats_workspace_bytes", N, L, M))
+        _lib.call("vmc_rbm_grad_stats", prec, _lib.ptr(flat), N, L, M, Wk, bk, _lib.ptr(w), _lib.ptr(E),
+                  _lib.ptr(emean), _lib.ptr(okMean), _lib.ptr(covOE), _lib.ptr(ws), ws.numel(), st)
+        x = complex(self.rhsPrefactor)
+        f = (-x) * covOE                       # complex form of F0 (tdvp.py:139)
+
+        # S = <O^dagger O>_c  (tdvp.py:142)
+        shift = float(self.diagonalShift) if (self.diagonalShift > 1e-10 and self.makeRealName != 'imag') else 0.0
+        A = self._gram(psi, flat, w, okMean, prec, N, L, M, P, Wk, bk, shift)
+
+        # eigendecomposition (tdvp.py:153-171), FP64 on the GPU
+        ev, U = torch.linalg.eigh(A)
+        if U.stride(0) != 1:
+            U = U.mT.contiguous().mT
+        vtf = torch.empty(P, dtype=torch.complex128, device=dev)
+        _lib.call("vmc_zgemv", 1, _lib.ptr(U), U.stride(1), P, _lib.ptr(f), _lib.ptr(vtf), st)
+
+        # SNR (tdvp.py:173-181)
+        snr = self._snr(psi, flat, w, okMean, E, emean, f, U, vtf, prec, N, L, M, P, Wk, bk)
+
+        # regularised pseudo-inverse (tdvp.py:183-213)
+        pinv = torch.empty(P, dtype=torch.float64, device=dev)
+        res = torch.empty(3, dtype=torch.float64, device=dev)
+        useSnr = not isinstance(self.sampler, ExactSampler)
+        _lib.call("vmc_tdvp_regularize", _lib.ptr(ev), _lib.ptr(vtf), _lib.ptr(snr) if useSnr else None, P,
+                  float(self.pinvCutoff), float(self.pinvTol), float(self.snrTol), _lib.ptr(pinv), _lib.ptr(res), st)
+        coef = (pinv.to(torch.complex128) * vtf).contiguous()
+        z = torch.empty(P, dtype=torch.complex128, device=dev)
+        _lib.call("vmc_zgemv", 0, _lib.ptr(U), U.stride(1), P, _lib.ptr(coef), _lib.ptr(z), st)
+
+        # bookkeeping in the reference's 2P layout
+        self._A, self._shift, self._z, self._covOE = A, shift, z, covOE
+        self.ev_c, self.V, self.VtF, self.snr_c = ev, U, vtf, snr
+        self.ElocMean = emean[0]
+        self.ElocVar = evar[0]
+        return self._realrep(psi, z), res[0], res[1]
+
+    def _realrep(self, psi, z):
+        """[Re z_leaf; Im z_leaf] per leaf (get_parameters layout, vqs.py:461-462)."""
+        parts = []
+        start = 0
+        for name, p in psi.params.items():
+            n = p.numel()
+            zz = z[start:start + n]
+            parts += [zz.real, zz.imag]
+            start += n
+        return torch.cat(parts)
+
+    def _gram(self, psi, flat, w, okMean, prec, N, L, M, P, Wk, bk, shift):
+        dev = flat.device
+        st = _lib.stream()
+        if self.precision == "mixed":
+            from . import gram as _gram
+            return _gram.mixed_hermitian(flat, w, okMean, prec, N, L, M, P, Wk, bk, shift)
+        fmt, dt = (0, torch.complex128) if self.precision == "fp64" else (1, torch.complex64)
+        X = torch.empty((N, P), dtype=dt, device=dev)
+        _lib.call("vmc_rbm_centered_gradients", prec, _lib.ptr(flat), N, L, M, Wk, bk, _lib.ptr(w),
+                  _lib.ptr(okMean), fmt, _lib.ptr(X), None, st)
+        A = torch.matmul(X.mH, X).to(torch.complex128)
+        del X
+        if shift:
+            A.diagonal().mul_(1.0 + shift)
+        return A
+
+    def _snr(self, psi, flat, w, okMean, E, emean, f, U, vtf, prec, N, L, M, P, Wk, bk):
+        dev = flat.device
+        st = _lib.stream()
+        x = complex(self.rhsPrefactor)
+        snr = torch.empty(P, dtype=torch.float64, device=dev)
+        if self.precision == "mixed":
+            from . import gram as _gram
+            colsq = _gram.mixed_snr_colsq(flat, w, okMean, E, emean, f, U, prec, N, L, M, P, Wk, bk, x)
+            realRep, cprec = 1, _lib.VMC_F32
+        else:
+            fmt, dt = (0, torch.complex128) if self.precision == "fp64" else (1, torch.complex64)
+            H = torch.empty((N, P), dtype=dt, device=dev)
+            _lib.call("vmc_rbm_snr_data", prec, _lib.ptr(flat), N, L, M, Wk, bk, _lib.ptr(w), _lib.ptr(okMean),
+                      _lib.ptr(E), _lib.ptr(emean), -x.real, -x.imag, _lib.ptr(f), fmt, _lib.ptr(H), None, st)
+            Y = torch.matmul(H, torch.conj(U).to(dt))
+            del H
+            colsq = (Y.real ** 2 + Y.imag ** 2).sum(0).to(torch.float64).contiguous()
+            del Y
+            realRep, cprec = 0, _lib.VMC_F64
+        self.rhoVar_c = torch.empty(P, dtype=torch.float64, device=dev)
+        _lib.call("vmc_tdvp_snr", _lib.ptr(vtf), cprec, _lib.ptr(colsq), P, realRep, float(mpi.globNumSamples),
+                  _lib.ptr(snr), _lib.ptr(self.rhoVar_c), st)
+        return snr
+
+    def _rbm_metadata(self, psi, update, residual, cutoff):
+        """tdvp_error (tdvp.py:102-104) and the 2P spectrum / SNR."""
+        z, A, shift = self._z, self._A, self._shift
+        Az = torch.mv(A, z)
+        if shift:
+            Az = Az - (shift / (1.0 + shift)) * A.diagonal() * z
+        zAz = torch.real(torch.vdot(z, Az))
+        x = complex(self.rhsPrefactor)
+        zF = torch.vdot(z, (-x) * self._covOE)
+        err = torch.abs(1. + (zAz - 2. * torch.real(zF)) / self.ElocVar0)
+        if self.makeRealName == 'imag':
+            spectrum = torch.cat([-torch.flip(self.ev_c, [0]), self.ev_c])
+            snr = torch.cat([torch.flip(self.snr_c, [0]), self.snr_c])
+        else:
+            spectrum = torch.repeat_interleave(self.ev_c, 2)
+            snr = torch.repeat_interleave(self.snr_c, 2)
+        self.ev = spectrum
+        self.snr = snr
+        return {"tdvp_error": err, "tdvp_residual": residual, "pinv_cutoff": cutoff, "SNR": snr,
+                "spectrum": spectrum}
+
+    # ===================================================== generic path
+    def get_tdvp_equation(self, Eloc, gradients):
+        """tdvp.py:134-148 on SampledObs inputs."""
+        self.ElocMean = Eloc.mean()[0]
+        self.ElocVar = Eloc.var()[0]
+        self.F0 = (-self.rhsPrefactor) * gradients.covar(Eloc).reshape(-1)
+        F = self.makeReal(self.F0)
+        self.S0 = gradients.covar()
+        S = self.makeReal(self.S0)
+        if self.diagonalShift > 1e-10:
+            S = S + torch.diag(self.diagonalShift * torch.diag(S))
+        return S, F
+
+    def _transform_to_eigenbasis(self, S, F):
+        self.ev, self.V = torch.linalg.eigh(S)
+        self.VtF = torch.matmul(torch.conj(self.V).T, F.to(self.V.dtype))
+
+    def _get_snr(self, Eloc, gradients):
+        EO = gradients.covar_data(Eloc).transform(linearFun=torch.conj(self.V).T,
+                                                  nonLinearFun=lambda v: transform_helper(v, self.rhsPrefactor,
+                                                                                          self.makeReal))
+        self.rhoVar = EO.var().reshape(-1)
+        self.snr = torch.sqrt(torch.abs(mpi.globNumSamples * (torch.conj(self.VtF) * self.VtF) / self.rhoVar)).reshape(-1)
+
+    def solve(self, Eloc, gradients):
+        """TDVP.solve (tdvp.py:183-213) for SampledObs inputs, in the 2P
+        representation (FP64, GPU)."""
+        self.S, F = self.get_tdvp_equation(Eloc, gradients)
+        self._transform_to_eigenbasis(self.S, F)
+        self._get_snr(Eloc, gradients)
+        ev = torch.real(self.ev) if self.ev.is_complex() else self.ev
+        self.invEv = torch.where(torch.abs(ev / ev[-1]) > 1e-14, 1. / ev, torch.zeros_like(ev))
+        residual = 1.0
+        cutoff = 1e-2
+        F_norm = torch.linalg.norm(F)
+        while residual > self.pinvTol and cutoff > self.pinvCutoff:
+            cutoff *= 0.8
+            regularizer = 1. / (1. + (max(cutoff, self.pinvCutoff) / torch.abs(ev / ev[-1])) ** 6)
+            if not isinstance(self.sampler, ExactSampler):
+                regularizer = regularizer * (1. / (1. + (self.snrTol / torch.real(self.snr)) ** 6))
+            pinvEv = self.invEv * regularizer
+            residual = float(torch.linalg.norm((pinvEv * ev - torch.ones_like(pinvEv)) * self.VtF) / F_norm)
+        update = torch.real(torch.matmul(self.V, (pinvEv.to(self.VtF.dtype) * self.VtF)))
+        return update, residual, max(cutoff, self.pinvCutoff)
+
+    def _get_tdvp_error(self, update):
+        """tdvp.py:102-104."""
+        u = update.to(self.S0.dtype)
+        return torch.abs(1. + torch.real(u.dot(self.S0.matmul(u)) - 2. * torch.real(u.dot(self.F0.to(u.dtype))))
+                         / self.ElocVar0)
+
+    # ========================================================== RHS
+    def __call__(self, netParameters, t, *, psi, hamiltonian, **rhsArgs):
+        """theta_dot = S^-1 F for the given parameters (tdvp.py:219-326)."""
+        tmpParameters = psi.get_parameters()
+        psi.set_parameters(netParameters)
+        numSamples = rhsArgs.get("numSamples", None)
+        outp = rhsArgs.get("outp", None)
+        configs, sampleLogPsi, p = self.sampler.sample(numSamples=numSamples)
+        fused = self._rbm_capable(psi, hamiltonian)
+        if fused:
+            Eloc = hamiltonian.get_O_loc_fused(configs, psi, None, t)
+            update, residual, cutoff = self._rbm_rhs(psi, configs, Eloc, p)
+        else:
+            Eloc = hamiltonian.get_O_loc(configs, psi, sampleLogPsi, t)
+            EObs = SampledObs(Eloc, p)
+            gObs = SampledObs(psi.gradients(configs), p)
+            update, residual, cutoff = self.solve(EObs, gObs)
+        psi.set_parameters(tmpParameters)
+        if rhsArgs.get("intStep", None) == 0:
+            self.ElocMean0 = self.ElocMean
+            self.ElocVar0 = self.ElocVar
+            if fused:
+                self.metaData = self._rbm_metadata(psi, update, residual, cutoff)
+                if self.crossValidation:
+                    self._cross_validate_rbm(psi, configs, Eloc, p, update, residual)
+            else:
+                self.metaData = {"tdvp_error": self._get_tdvp_error(update), "tdvp_residual": residual,
+                                 "pinv_cutoff": cutoff, "SNR": self.snr, "spectrum": self.ev}
+                if self.crossValidation:
+                    raise NotImplementedError("cross-validation is implemented for the fused CpxRBM path")
+        return update
+
+    def _cross_validate_rbm(self, psi, configs, Eloc, p, update, residual):
+        """Cross-validation of tdvp.py:230-248: solve on the even samples,
+        check on the odd ones.  A subset is the same sample with the other
+        half's weights set to 0 and the rest renormalised (stats.py:310-329)."""
+        w = p.reshape(-1)
+        idx = torch.arange(w.numel(), device=w.device)
+        w1 = torch.where(idx % 2 == 0, w, torch.zeros_like(w))
+        w2 = torch.where(idx % 2 == 1, w, torch.zeros_like(w))
+        w1 = w1 / w1.sum()
+        w2 = w2 / w2.sum()
+        saved = (self._A, self._shift, self._z, self._covOE, self.ev_c, self.V, self.VtF, self.snr_c,
+                 self.ElocMean, self.ElocVar)
+        update1, _, _ = self._rbm_rhs(psi, configs, Eloc, p, weights=w1)
+        z1 = self._z
+        # tdvp error of update_1 against the full-sample S0, F0 and ElocVar0
+        (self._A, self._shift, self._z, self._covOE) = saved[:4]
+        Az1 = torch.mv(self._A, z1)
+        if self._shift:
+            Az1 = Az1 - (self._shift / (1.0 + self._shift)) * self._A.diagonal() * z1
+        x = complex(self.rhsPrefactor)
+        err1 = torch.abs(1. + (torch.real(torch.vdot(z1, Az1)) - 2. * torch.real(torch.vdot(z1, (-x) * self._covOE)))
+                         / self.ElocVar0)
+        # residual of update_1 on the odd half: ||S2 u1 - F2|| / ||F2||
+        self._rbm_rhs(psi, configs, Eloc, p, weights=w2)
+        A2, z2shift, cov2 = self._A, self._shift, self._covOE
+        r = torch.mv(A2, z1) - (-x) * cov2
+        valRes = (torch.linalg.norm(r) / torch.linalg.norm((-x) * cov2)) / residual
+        (self._A, self._shift, self._z, self._covOE, self.ev_c, self.V, self.VtF, self.snr_c,
+         self.ElocMean, self.ElocVar) = saved
+        self.crossValidationFactor_residual = valRes
+        self.crossValidationFactor_tdvpErr = err1 / self.metaData["tdvp_error"]
+        self.metaData["tdvp_residual_cross_validation_ratio"] = self.crossValidationFactor_residual
+        self.metaData["tdvp_error_cross_validation_ratio"] = self.crossValidationFactor_tdvpErr
