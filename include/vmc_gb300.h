@@ -221,10 +221,13 @@ typedef enum {
                         * (N, 2P) for SNR data; value ~ hi + lo            */
 } vmc_data_format;
 
-/* X_nk = sqrt(w_n) (O_nk - ok_mean_k), O in the compact layout. */
+/* X_nk = sqrt(w_n) (O_nk - ok_mean_k), O in the compact layout; ld_out is
+ * the leading dimension (elements) of the output rows (>= P for C128/C64,
+ * >= N for the transposed BF16X2 planes). */
 int vmc_rbm_centered_gradients(int32_t precision, const int32_t* configs, int64_t num_configs, int32_t num_sites,
                                int32_t num_hidden, const void* kernel, const void* bias, const double* weights,
-                               const double* ok_mean, int32_t format, void* out, void* out_lo, vmc_stream_t stream);
+                               const double* ok_mean, int32_t format, void* out, void* out_lo, int64_t ld_out,
+                               vmc_stream_t stream);
 
 /* H_nk = sqrt(w_n) ((neg_rhs) (E_n - Ebar) conj(O_nk - ok_mean_k) - force_k): the
  * per-sample data of covar_data(O, E).transform(makeReal(-x .)) before the
@@ -234,7 +237,7 @@ int vmc_rbm_snr_data(int32_t precision, const int32_t* configs, int64_t num_conf
                      int32_t num_hidden, const void* kernel, const void* bias, const double* weights,
                      const double* ok_mean, const double* eloc, const double* eloc_mean, double neg_rhs_re,
                      double neg_rhs_im, const double* force, int32_t format, void* out, void* out_lo,
-                     vmc_stream_t stream);
+                     int64_t ld_out, vmc_stream_t stream);
 
 /* ------------------------------------------------------------------------
  * TDVP solve helpers (util/tdvp.py:134-213), complex P-dimensional form.
@@ -261,6 +264,37 @@ int vmc_tdvp_snr(const double* vtf, int32_t colsq_precision, const void* colsq, 
  * snr NULL = exact sampling (no SNR factor). ev ascending. */
 int vmc_tdvp_regularize(const double* ev, const double* vtf, const double* snr, int32_t n, double pinv_cutoff,
                         double pinv_tol, double snr_tol, double* pinv, double* result, vmc_stream_t stream);
+
+/* ------------------------------------------------------------------------
+ * Split-precision BF16 contractions on the tcgen05 tensor cores (FP32
+ * accumulation in TMEM): x ~ hi + lo, products hi.hi + hi.lo + lo.hi.
+ * Operand planes are bf16, row-major with leading dimension ld (elements,
+ * a multiple of 8, rows 16-byte aligned); the reduction index is contiguous.
+ * ------------------------------------------------------------------------ */
+
+/* S build (stats.py:52-58 via tdvp.py:142): gram = R R^T for R (rows x k)
+ * given as hi/lo planes; fp32 output (rows x rows, leading dimension ld_gram,
+ * a multiple of 4); only 128x256 tiles touching the upper triangle
+ * (row <= col) are written. */
+int vmc_gram_bf16x3(const void* hi, const void* lo, int32_t rows, int32_t k, int64_t ld, float* gram,
+                    int64_t ld_gram, vmc_stream_t stream);
+
+/* SNR transform (stats.py:75-83 via tdvp.py:175-179): colsq[c] =
+ * sum_r (sum_j A[r][j] B[c][j])^2 for A (m x k) and B (n x k) given as hi/lo
+ * planes; colsq (n floats) is overwritten; the product is never stored. */
+int vmc_gemm_bf16x3_colsq(const void* a_hi, const void* a_lo, int32_t m, int64_t lda, const void* b_hi,
+                          const void* b_lo, int32_t n, int64_t ldb, int32_t k, float* colsq, vmc_stream_t stream);
+
+/* Error flag of the tensor-core kernels (a bounded wait that ran out);
+ * synchronises the device.  reset != 0 clears it. */
+int vmc_tc_error_flag(int32_t reset);
+
+/* B^T planes (2P x 2P, leading dimension ld) of the real representation
+ * [[Re U, -Im U], [Im U, Re U]] of the eigenvectors U (P x P, column-major
+ * c128, leading dimension ldu), split into bf16 hi/lo: the B operand of the
+ * SNR contraction. */
+int vmc_eigvec_bf16x2(const double* U, int64_t ldu, int32_t num_params, void* bt_hi, void* bt_lo, int64_t ld,
+                      vmc_stream_t stream);
 
 #ifdef __cplusplus
 }

@@ -72,7 +72,9 @@ def test_exact_basis_bit_exact(cuda, L, ldim):
 # ---------------------------------------------------------------- network
 @pytest.mark.parametrize("L,M,bias", [(10, 20, True), (4, 2, False), (64, 256, True), (37, 13, True)])
 def test_rbm_logpsi_and_gradients(cuda, L, M, bias):
-    psi, opsi = _rbm_pair(L, M, bias, seed=L * M)
+    # weights scaled so that theta stays clear of the poles of tanh (i pi/2),
+    # where summation-order rounding of theta is amplified
+    psi, opsi = _rbm_pair(L, M, bias, seed=L * M, scale=0.3 / np.sqrt(L))
     s = _configs(300, L, seed=1)
     lp = psi(s).cpu().numpy()
     assert _rel(lp, opsi(s)) < 1e-12

@@ -115,10 +115,24 @@ def load(build_if_missing=True):
         return lib
 
 
+# kernels launched by one successful call of each entry point
+KERNELS_PER_CALL = {
+    "vmc_exact_basis": 1, "vmc_exact_probabilities": 2, "vmc_mc_probabilities": 2, "vmc_rbm_prepare": 1,
+    "vmc_rbm_logpsi": 1, "vmc_rbm_gradients": 1, "vmc_rbm_metropolis": 1, "vmc_bf_matrix_elements": 1,
+    "vmc_bf_gather": 1, "vmc_oloc_from_sprimes": 1, "vmc_rbm_oloc_fused": 1, "vmc_weighted_mean_var": 3,
+    "vmc_rbm_grad_stats": 3, "vmc_rbm_centered_gradients": 1, "vmc_rbm_snr_data": 1, "vmc_gram_to_hermitian": 1,
+    "vmc_zgemv": 1, "vmc_tdvp_snr": 1, "vmc_tdvp_regularize": 1, "vmc_gram_bf16x3": 1,
+    "vmc_gemm_bf16x3_colsq": 1, "vmc_eigvec_bf16x2": 1,
+}
+launch_count = 0
+
+
 def call(name, *args):
     """Call a status-returning entry point; raise VmcError on failure."""
+    global launch_count
     lib = load()
     rc = getattr(lib, name)(*args)
+    launch_count += KERNELS_PER_CALL.get(name, 1)
     if rc != 0:
         msg = lib.vmc_last_error_string().decode(errors="replace")
         raise VmcError(f"{name} failed with status {rc}: {msg}")

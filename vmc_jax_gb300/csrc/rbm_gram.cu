@@ -63,6 +63,7 @@ struct data_args {
   const double2* force;    // (P) f_k = -x * covar(O,E)_k (SNR data) or null
   int format;
   int tileN;  // samples per block
+  int64_t ld; // leading dimension of the output (elements)
   void* out;
   void* out2;              // lo plane for BF16X2
 };
@@ -117,10 +118,10 @@ __global__ void __launch_bounds__(256) rbm_data_kernel(const int32_t* __restrict
         cpx<double> v = data_value<T>(a, tt, sg, r, n, k, sw);
         float vr = (float)v.re, vi = (float)v.im;
         __nv_bfloat16 hr = __float2bfloat16_rn(vr), hi_ = __float2bfloat16_rn(vi);
-        hi[(size_t)k * a.N + n] = hr;
-        lo[(size_t)k * a.N + n] = __float2bfloat16_rn(vr - __bfloat162float(hr));
-        hi[(size_t)(P + k) * a.N + n] = hi_;
-        lo[(size_t)(P + k) * a.N + n] = __float2bfloat16_rn(vi - __bfloat162float(hi_));
+        hi[(size_t)k * a.ld + n] = hr;
+        lo[(size_t)k * a.ld + n] = __float2bfloat16_rn(vr - __bfloat162float(hr));
+        hi[(size_t)(P + k) * a.ld + n] = hi_;
+        lo[(size_t)(P + k) * a.ld + n] = __float2bfloat16_rn(vi - __bfloat162float(hi_));
       }
     }
     return;
@@ -133,18 +134,18 @@ __global__ void __launch_bounds__(256) rbm_data_kernel(const int32_t* __restrict
     for (int k = tid; k < P; k += blockDim.x) {
       cpx<double> v = data_value<T>(a, tt, sg, r, n, k, sw);
       if (a.format == VMC_DATA_C128) {
-        reinterpret_cast<double2*>(a.out)[n * P + k] = make_double2(v.re, v.im);
+        reinterpret_cast<double2*>(a.out)[n * a.ld + k] = make_double2(v.re, v.im);
       } else if (a.format == VMC_DATA_C64) {
-        reinterpret_cast<float2*>(a.out)[n * P + k] = make_float2((float)v.re, (float)v.im);
+        reinterpret_cast<float2*>(a.out)[n * a.ld + k] = make_float2((float)v.re, (float)v.im);
       } else {  // BF16X2 row-major (N, 2P)
         __nv_bfloat16* hi = reinterpret_cast<__nv_bfloat16*>(a.out);
         __nv_bfloat16* lo = reinterpret_cast<__nv_bfloat16*>(a.out2);
         float vr = (float)v.re, vi = (float)v.im;
         __nv_bfloat16 hr = __float2bfloat16_rn(vr), hi_ = __float2bfloat16_rn(vi);
-        hi[n * 2 * P + k] = hr;
-        lo[n * 2 * P + k] = __float2bfloat16_rn(vr - __bfloat162float(hr));
-        hi[n * 2 * P + P + k] = hi_;
-        lo[n * 2 * P + P + k] = __float2bfloat16_rn(vi - __bfloat162float(hi_));
+        hi[n * a.ld + k] = hr;
+        lo[n * a.ld + k] = __float2bfloat16_rn(vr - __bfloat162float(hr));
+        hi[n * a.ld + P + k] = hi_;
+        lo[n * a.ld + P + k] = __float2bfloat16_rn(vi - __bfloat162float(hi_));
       }
     }
   }
@@ -162,6 +163,12 @@ static int launch_data(int32_t precision, const int32_t* configs, const void* ke
   VMC_REQUIRE(a.out && (a.format != VMC_DATA_BF16X2 || a.out2), VMC_ERR_INVALID_ARGUMENT, "%s: null output", fn);
   VMC_REQUIRE(a.N > 0 && a.L > 0 && a.M > 0 && configs && kernel && a.w && a.okMean, VMC_ERR_INVALID_ARGUMENT,
               "%s: bad arguments", fn);
+  {
+    const int64_t P = (int64_t)a.M * a.L + (a.hasBias ? a.M : 0);
+    const int64_t need = a.format == VMC_DATA_BF16X2 ? (a.eloc ? 2 * P : a.N) : P;
+    VMC_REQUIRE(a.ld >= need, VMC_ERR_INVALID_ARGUMENT, "%s: leading dimension %lld < %lld", fn, (long long)a.ld,
+                (long long)need);
+  }
   const size_t el = precision == VMC_F64 ? 16 : 8;
   int kTileN = 64;
   while (kTileN > 8 && (size_t)kTileN * (a.M * el + a.L) > 200 * 1024) kTileN /= 2;
@@ -187,7 +194,7 @@ static int launch_data(int32_t precision, const int32_t* configs, const void* ke
 extern "C" int vmc_rbm_centered_gradients(int32_t precision, const int32_t* configs, int64_t num_configs,
                                           int32_t num_sites, int32_t num_hidden, const void* kernel, const void* bias,
                                           const double* weights, const double* ok_mean, int32_t format, void* out,
-                                          void* out_lo, vmc_stream_t stream) {
+                                          void* out_lo, int64_t ld_out, vmc_stream_t stream) {
   data_args a;
   a.N = num_configs;
   a.L = num_sites;
@@ -202,6 +209,7 @@ extern "C" int vmc_rbm_centered_gradients(int32_t precision, const int32_t* conf
   a.format = format;
   a.out = out;
   a.out2 = out_lo;
+  a.ld = ld_out;
   return launch_data(precision, configs, kernel, bias, a, stream, "vmc_rbm_centered_gradients");
 }
 
@@ -209,7 +217,7 @@ extern "C" int vmc_rbm_snr_data(int32_t precision, const int32_t* configs, int64
                                 int32_t num_hidden, const void* kernel, const void* bias, const double* weights,
                                 const double* ok_mean, const double* eloc, const double* eloc_mean,
                                 double neg_rhs_re, double neg_rhs_im, const double* force, int32_t format, void* out,
-                                void* out_lo, vmc_stream_t stream) {
+                                void* out_lo, int64_t ld_out, vmc_stream_t stream) {
   VMC_REQUIRE(eloc && eloc_mean && force, VMC_ERR_INVALID_ARGUMENT, "vmc_rbm_snr_data: null argument");
   data_args a;
   a.N = num_configs;
@@ -225,5 +233,6 @@ extern "C" int vmc_rbm_snr_data(int32_t precision, const int32_t* configs, int64
   a.format = format;
   a.out = out;
   a.out2 = out_lo;
+  a.ld = ld_out;
   return launch_data(precision, configs, kernel, bias, a, stream, "vmc_rbm_snr_data");
 }

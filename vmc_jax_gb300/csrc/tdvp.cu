@@ -190,3 +190,38 @@ extern "C" int vmc_tdvp_snr(const double* vtf, int32_t colsq_precision, const vo
                                                              num_samples, snr, rho_var);
   return check_launch("vmc_tdvp_snr");
 }
+
+#include <cuda_bf16.h>
+
+namespace vmc {
+// Bt[c][k] = B[k][c] with B = [[Ur, -Ui], [Ui, Ur]] (U column-major: U_jk at k*ldu + j).
+__global__ void eigvec_bf16x2_kernel(const double2* __restrict__ U, int64_t ldu, int P, __nv_bfloat16* __restrict__ hi,
+                                     __nv_bfloat16* __restrict__ lo, int64_t ld) {
+  const int64_t n2 = 2 * (int64_t)P;
+  const int64_t total = n2 * n2;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int c = (int)(t / n2), k = (int)(t - (t / n2) * n2);
+    const int cc = c < P ? c : c - P, kk = k < P ? k : k - P;
+    const double2 u = U[(int64_t)cc * ldu + kk];
+    double v;
+    if (c < P) v = k < P ? u.x : u.y;
+    else v = k < P ? -u.y : u.x;
+    const float f = (float)v;
+    const __nv_bfloat16 h = __float2bfloat16_rn(f);
+    hi[(int64_t)c * ld + k] = h;
+    lo[(int64_t)c * ld + k] = __float2bfloat16_rn(f - __bfloat162float(h));
+  }
+}
+}  // namespace vmc
+
+extern "C" int vmc_eigvec_bf16x2(const double* U, int64_t ldu, int32_t num_params, void* bt_hi, void* bt_lo,
+                                 int64_t ld, vmc_stream_t stream) {
+  VMC_REQUIRE(U && bt_hi && bt_lo && num_params > 0 && ldu >= num_params && ld >= 2 * (int64_t)num_params,
+              VMC_ERR_INVALID_ARGUMENT, "vmc_eigvec_bf16x2: bad arguments");
+  const int64_t total = 4 * (int64_t)num_params * num_params;
+  const int blocks = (int)std::min<int64_t>((total + 255) / 256, 152 * 32);
+  eigvec_bf16x2_kernel<<<blocks, 256, 0, as_stream(stream)>>>(reinterpret_cast<const double2*>(U), ldu, num_params,
+                                                              reinterpret_cast<__nv_bfloat16*>(bt_hi),
+                                                              reinterpret_cast<__nv_bfloat16*>(bt_lo), ld);
+  return check_launch("vmc_eigvec_bf16x2");
+}

@@ -56,6 +56,8 @@ __device__ __forceinline__ T abs2(cpx<T> a) { return a.re * a.re + a.im * a.im; 
 
 __device__ __forceinline__ float fexp(float x) { return expf(x); }
 __device__ __forceinline__ double fexp(double x) { return exp(x); }
+__device__ __forceinline__ float fexpm1(float x) { return expm1f(x); }
+__device__ __forceinline__ double fexpm1(double x) { return expm1(x); }
 __device__ __forceinline__ float flog1p(float x) { return log1pf(x); }
 __device__ __forceinline__ double flog1p(double x) { return log1p(x); }
 __device__ __forceinline__ float flog(float x) { return logf(x); }
@@ -100,13 +102,14 @@ template <typename T>
 __device__ __forceinline__ cpx<T> ctanh_(cpx<T> x) {
   bool neg = signbit(x.re);
   T a = neg ? -x.re : x.re;
-  T e = fexp(T(-2) * a);  // in (0, 1]
+  // tanh(a + ib) = (1 - e^2 + 2 i e sin 2b) / (1 + e^2 + 2 e cos 2b), e = exp(-2a);
+  // 1 - e^2 = -em (2 + em) with em = expm1(-2a) keeps full precision for small a
+  T em = fexpm1(T(-2) * a);
+  T e = T(1) + em;
   T s2, c2;
   fsincos(T(2) * x.im, &s2, &c2);
-  // tanh(a + ib) = (1 - e^2 + 2 i e sin 2b) / (1 + e^2 + 2 e cos 2b)
-  T e2 = e * e;
-  T den = T(1) + e2 + T(2) * e * c2;
-  T re = (T(1) - e2) / den;
+  T den = T(1) + e * e + T(2) * e * c2;
+  T re = -em * (T(2) + em) / den;
   T im = T(2) * e * s2 / den;
   return mk(neg ? -re : re, im);
 }

@@ -32,6 +32,7 @@ from .. import global_defs
 from .. import mpi_wrapper as mpi
 from ..sampler import ExactSampler
 from ..stats import SampledObs
+from .timing import TIMER
 
 
 def realFun(x):
@@ -140,6 +141,7 @@ class TDVP:
         Wk, bk = _lib.ptr(params["kernel"]), _lib.ptr(params.get("bias"))
 
         # E_loc statistics (stats.py:197-205, 248-252)
+        TIMER.mark("statistics")
         emean = torch.empty(1, dtype=torch.complex128, device=dev)
         evar = torch.empty(1, dtype=torch.float64, device=dev)
         ws = _lib.Workspace.get(_lib.query("vmc_reduce_workspace_bytes", 2))
@@ -156,9 +158,11 @@ class TDVP:
 
         # S = <O^dagger O>_c  (tdvp.py:142)
         shift = float(self.diagonalShift) if (self.diagonalShift > 1e-10 and self.makeRealName != 'imag') else 0.0
+        TIMER.mark("s_build")
         A = self._gram(psi, flat, w, okMean, prec, N, L, M, P, Wk, bk, shift)
 
         # eigendecomposition (tdvp.py:153-171), FP64 on the GPU
+        TIMER.mark("eigh")
         ev, U = torch.linalg.eigh(A)
         if U.stride(0) != 1:
             U = U.mT.contiguous().mT
@@ -166,9 +170,11 @@ class TDVP:
         _lib.call("vmc_zgemv", 1, _lib.ptr(U), U.stride(1), P, _lib.ptr(f), _lib.ptr(vtf), st)
 
         # SNR (tdvp.py:173-181)
+        TIMER.mark("snr")
         snr = self._snr(psi, flat, w, okMean, E, emean, f, U, vtf, prec, N, L, M, P, Wk, bk)
 
         # regularised pseudo-inverse (tdvp.py:183-213)
+        TIMER.mark("solve")
         pinv = torch.empty(P, dtype=torch.float64, device=dev)
         res = torch.empty(3, dtype=torch.float64, device=dev)
         useSnr = not isinstance(self.sampler, ExactSampler)
@@ -205,7 +211,7 @@ class TDVP:
         fmt, dt = (0, torch.complex128) if self.precision == "fp64" else (1, torch.complex64)
         X = torch.empty((N, P), dtype=dt, device=dev)
         _lib.call("vmc_rbm_centered_gradients", prec, _lib.ptr(flat), N, L, M, Wk, bk, _lib.ptr(w),
-                  _lib.ptr(okMean), fmt, _lib.ptr(X), None, st)
+                  _lib.ptr(okMean), fmt, _lib.ptr(X), None, P, st)
         A = torch.matmul(X.mH, X).to(torch.complex128)
         del X
         if shift:
@@ -225,7 +231,7 @@ class TDVP:
             fmt, dt = (0, torch.complex128) if self.precision == "fp64" else (1, torch.complex64)
             H = torch.empty((N, P), dtype=dt, device=dev)
             _lib.call("vmc_rbm_snr_data", prec, _lib.ptr(flat), N, L, M, Wk, bk, _lib.ptr(w), _lib.ptr(okMean),
-                      _lib.ptr(E), _lib.ptr(emean), -x.real, -x.imag, _lib.ptr(f), fmt, _lib.ptr(H), None, st)
+                      _lib.ptr(E), _lib.ptr(emean), -x.real, -x.imag, _lib.ptr(f), fmt, _lib.ptr(H), None, P, st)
             Y = torch.matmul(H, torch.conj(U).to(dt))
             del H
             colsq = (Y.real ** 2 + Y.imag ** 2).sum(0).to(torch.float64).contiguous()
@@ -315,11 +321,14 @@ class TDVP:
         psi.set_parameters(netParameters)
         numSamples = rhsArgs.get("numSamples", None)
         outp = rhsArgs.get("outp", None)
+        TIMER.mark("sampling")
         configs, sampleLogPsi, p = self.sampler.sample(numSamples=numSamples)
         fused = self._rbm_capable(psi, hamiltonian)
         if fused:
+            TIMER.mark("eloc")
             Eloc = hamiltonian.get_O_loc_fused(configs, psi, None, t)
             update, residual, cutoff = self._rbm_rhs(psi, configs, Eloc, p)
+            TIMER.mark("rhs_end")
         else:
             Eloc = hamiltonian.get_O_loc(configs, psi, sampleLogPsi, t)
             EObs = SampledObs(Eloc, p)

@@ -1,0 +1,38 @@
+"""Per-phase GPU timing of the TDVP step with CUDA events on the current
+stream (off unless enabled; used by the benchmark)."""
+
+import torch
+
+
+class PhaseTimer:
+    def __init__(self):
+        self.enabled = False
+        self.marks = []
+
+    def reset(self):
+        self.marks = []
+
+    def mark(self, name):
+        if self.enabled:
+            ev = torch.cuda.Event(enable_timing=True)
+            ev.record()
+            self.marks.append((name, ev))
+
+    def durations(self):
+        """{phase: total ms} where a phase runs from its mark to the next mark
+        ("<name>_end" marks close a phase without opening one)."""
+        torch.cuda.synchronize()
+        out = {}
+        for (n0, e0), (n1, e1) in zip(self.marks[:-1], self.marks[1:]):
+            if n0.endswith("_end"):
+                continue
+            out[n0] = out.get(n0, 0.0) + e0.elapsed_time(e1)
+        return out
+
+    def spans(self, name):
+        """Durations (ms) of every occurrence of ``name`` ... next mark."""
+        torch.cuda.synchronize()
+        return [e0.elapsed_time(e1) for (n0, e0), (n1, e1) in zip(self.marks[:-1], self.marks[1:]) if n0 == name]
+
+
+TIMER = PhaseTimer()

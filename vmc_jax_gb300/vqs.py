@@ -67,8 +67,9 @@ class NQS:
         self.parameters = {"params": self.net.init(self.seed, sampleShape, global_defs.device())}
         self.holomorphic = bool(self.net.holomorphic)
         self.realParams = bool(self.net.realParams)
-        self.paramShapes = [(int(p.numel()), tuple(p.shape)) for p in self.params.values()]
-        self.numParameters = int(sum(p.numel() for p in self.params.values()))
+        leaves = self.parameters["params"]
+        self.paramShapes = [(int(p.numel()), tuple(p.shape)) for p in leaves.values()]
+        self.numParameters = int(sum(p.numel() for p in leaves.values()))
         self.initialized = True
 
     @property
