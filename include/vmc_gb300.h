@@ -133,6 +133,16 @@ int vmc_metropolis_draws_host(uint64_t seed, uint32_t call_index, uint32_t step,
 int vmc_mc_probabilities(const double* log_psi, int64_t num_samples, double factor, double* p, void* workspace,
                          size_t workspace_bytes, vmc_stream_t stream);
 
+/* Vector-Jacobian product of log psi: out_k = sum_n conj(g_n) O_nk (c128, compact
+ * layout) for a cotangent g (N, c128), without materialising O: the
+ * activations tanh(theta) are recomputed from the configurations.  The
+ * backward of a torch.autograd.Function / jax.custom_vjp over log psi.
+ * workspace: vmc_rbm_vjp_workspace_bytes. */
+size_t vmc_rbm_vjp_workspace_bytes(int64_t num_configs, int32_t num_sites, int32_t num_hidden);
+int vmc_rbm_vjp(int32_t precision, const int32_t* configs, int64_t num_configs, int32_t num_sites,
+                int32_t num_hidden, const void* kernel, const void* bias, const double* cotangent, double* out,
+                void* workspace, size_t workspace_bytes, vmc_stream_t stream);
+
 /* ------------------------------------------------------------------------
  * Branch-free operators (operator/branch_free.py:311-487).
  * The tables are those of BranchFreeOperator.compile (348-414): every
@@ -295,6 +305,46 @@ int vmc_tc_error_flag(int32_t reset);
  * SNR contraction. */
 int vmc_eigvec_bf16x2(const double* U, int64_t ldu, int32_t num_params, void* bt_hi, void* bt_lo, int64_t ld,
                       vmc_stream_t stream);
+
+/* ------------------------------------------------------------------------
+ * Real CNN (nets/cnn.py:18-83): periodic padding (0, F-1), VALID
+ * cross-correlation with HWIO kernels, unit strides, activation after every
+ * layer (0: x^2/2 - x^4/12, 1: poly6, 2: x^2, 3: poly5), output
+ * sum / sqrt(#elements).  Parameters: one flat real array (f64 or f32) in
+ * jVMC's leaf order -- per layer Conv_l/bias (if present) then Conv_l/kernel
+ * raveled (F..., C_in, C_out).  Configurations: (N, dims...) row-major.
+ * ------------------------------------------------------------------------ */
+typedef struct {
+  int32_t ndim;           /* 1 or 2                                      */
+  int32_t dims[2];        /* lattice extent(s)                           */
+  int32_t filter[2];      /* filter diameter(s)                          */
+  int32_t num_layers;     /* 1..4                                        */
+  int32_t channels[4];
+  int32_t activation[4];
+  int32_t has_bias[4];
+} vmc_cnn_desc;
+
+/* Number of real parameters of the network (-1 on an invalid descriptor). */
+int vmc_cnn_num_params(const vmc_cnn_desc* desc);
+
+/* log psi (real, returned as c128 with imaginary part 0); replaces
+ * NQS._eval for a CNN (vqs.py:242-251, cnn.py:41-81). */
+int vmc_cnn_logpsi(int32_t precision, const vmc_cnn_desc* desc, const int32_t* configs, int64_t num_configs,
+                   const void* params, double* log_psi, vmc_stream_t stream);
+
+/* d log psi / d theta per configuration by a hand-written backward pass that
+ * recomputes the activations of each configuration in shared memory
+ * (flat_gradient, vqs.py:46-51).  layout VMC_GRAD_REFERENCE: (N, P) c128
+ * with imaginary part 0; VMC_GRAD_COMPACT: (N, P) f64. */
+int vmc_cnn_gradients(int32_t precision, const vmc_cnn_desc* desc, const int32_t* configs, int64_t num_configs,
+                      const void* params, int32_t layout, double* out, vmc_stream_t stream);
+
+/* Metropolis sampling for the CNN with full re-evaluation of each proposal
+ * (sampler.py:264-358); random stream and arguments as vmc_rbm_metropolis. */
+int vmc_cnn_metropolis(int32_t precision, const vmc_cnn_desc* desc, int32_t* states, int32_t num_chains,
+                       const void* params, double mu, uint64_t seed, uint32_t call_index, int64_t therm_steps,
+                       int64_t sweep_steps, int64_t samples_per_chain, int32_t* configs_out, void* counters,
+                       vmc_stream_t stream);
 
 #ifdef __cplusplus
 }

@@ -59,6 +59,8 @@ def _ctype(decl):
         inner = base.rstrip("*").strip()
         if inner == "vmc_bf_operator":
             return ctypes.POINTER(BfOperator)
+        if inner == "vmc_cnn_desc":
+            return ctypes.c_void_p
         if inner == "char":
             return ctypes.c_char_p
         return ctypes.c_void_p
@@ -122,7 +124,8 @@ KERNELS_PER_CALL = {
     "vmc_bf_gather": 1, "vmc_oloc_from_sprimes": 1, "vmc_rbm_oloc_fused": 1, "vmc_weighted_mean_var": 3,
     "vmc_rbm_grad_stats": 3, "vmc_rbm_centered_gradients": 1, "vmc_rbm_snr_data": 1, "vmc_gram_to_hermitian": 1,
     "vmc_zgemv": 1, "vmc_tdvp_snr": 1, "vmc_tdvp_regularize": 1, "vmc_gram_bf16x3": 1,
-    "vmc_gemm_bf16x3_colsq": 1, "vmc_eigvec_bf16x2": 1,
+    "vmc_gemm_bf16x3_colsq": 1, "vmc_eigvec_bf16x2": 1, "vmc_cnn_logpsi": 1, "vmc_cnn_gradients": 1,
+    "vmc_cnn_metropolis": 1, "vmc_rbm_vjp": 4,
 }
 launch_count = 0
 
@@ -142,6 +145,11 @@ def call(name, *args):
 def query(name, *args):
     """Call a value-returning entry point (sizes, version)."""
     return getattr(load(), name)(*args)
+
+
+def ctypes_ref(struct):
+    """Address of a ctypes structure for a ``const T*`` argument."""
+    return ctypes.addressof(struct)
 
 
 def ptr(t):

@@ -310,11 +310,14 @@ constexpr int kStatChunks = 32;
 //   force rows: c_n * sigma_ni * conj(t_nj)      (c_n = w_n (E_n - Ebar))
 // for the bias row (sigma = 1, row 0) and every site row (rows 1..L).
 // blockDim = (32 hidden lanes, kStatSiteGroups); grid = (ceil(M/32), chunks).
+// acoef (optional): complex per-sample coefficients a_n replacing w_n in the
+// mean rows (used by the vector-Jacobian product with a_n = conj(g_n)).
 __global__ void rbm_stats_partial_kernel(const int32_t* __restrict__ configs, const double2* __restrict__ tanhT,
                                          const double* __restrict__ w, const double2* __restrict__ eloc,
                                          const double2* __restrict__ emean, int64_t N, int L, int M,
                                          double2* __restrict__ partial /* (chunks, 2, L+1, M) */,
-                                         double2* __restrict__ csum_partial /* (chunks) */) {
+                                         double2* __restrict__ csum_partial /* (chunks) */,
+                                         const double2* __restrict__ acoef) {
   const int lane = threadIdx.x, grp = threadIdx.y;
   const int j = blockIdx.x * 32 + lane;
   const int rows = L + 1;
@@ -323,7 +326,7 @@ __global__ void rbm_stats_partial_kernel(const int32_t* __restrict__ configs, co
   const int64_t chunk = (N + gridDim.y - 1) / gridDim.y;
   const int64_t n0 = blockIdx.y * chunk;
   const int64_t n1 = min(N, n0 + chunk);
-  const double2 em = *emean;
+  const double2 em = eloc ? *emean : make_double2(0.0, 0.0);
   constexpr int RMAX = 12;  // rows per group held in registers per pass
   double2 cs = make_double2(0.0, 0.0);
   for (int rb = r0; rb < min(rows, r0 + rowsPerGrp); rb += RMAX) {
@@ -332,8 +335,8 @@ __global__ void rbm_stats_partial_kernel(const int32_t* __restrict__ configs, co
 #pragma unroll
     for (int q = 0; q < RMAX; ++q) mre[q] = mim[q] = fre[q] = fim[q] = 0.0;
     for (int64_t n = n0; n < n1; ++n) {
-      const double a = w[n];
-      const double2 e = eloc[n];
+      const double a = acoef ? 0.0 : w[n];
+      const double2 e = eloc ? eloc[n] : make_double2(0.0, 0.0);
       const double cr = a * (e.x - em.x), ci = a * (e.y - em.y);
       if (rb == r0 && grp == 0 && lane == 0 && blockIdx.x == 0) {
         cs.x += cr;
@@ -341,7 +344,12 @@ __global__ void rbm_stats_partial_kernel(const int32_t* __restrict__ configs, co
       }
       if (j >= M) continue;
       const double2 t = tanhT[n * M + j];
-      const double ar = a * t.x, ai = a * t.y;
+      double ar = a * t.x, ai = a * t.y;
+      if (acoef) {
+        const double2 z = acoef[n];
+        ar = z.x * t.x - z.y * t.y;
+        ai = z.x * t.y + z.y * t.x;
+      }
       // c * conj(t)
       const double fr = cr * t.x + ci * t.y, fi = ci * t.x - cr * t.y;
       const int32_t* s = configs + n * L;
@@ -594,7 +602,7 @@ extern "C" int vmc_rbm_grad_stats(int32_t precision, const int32_t* configs, int
   dim3 grd((num_hidden + 31) / 32, kStatChunks);
   rbm_stats_partial_kernel<<<grd, blk, 0, st>>>(configs, tanhT, weights, reinterpret_cast<const double2*>(eloc),
                                                 reinterpret_cast<const double2*>(eloc_mean), num_configs, num_sites,
-                                                num_hidden, partial, csum);
+                                                num_hidden, partial, csum, nullptr);
   rc = check_launch("vmc_rbm_grad_stats(partial)");
   if (rc) return rc;
   int64_t outs = (int64_t)(num_sites + 1) * num_hidden;
@@ -786,4 +794,79 @@ extern "C" int vmc_rbm_metropolis(int32_t precision, int32_t* states, int32_t nu
   return dispatch_metropolis<float>(states, num_chains, make_params<float>(kernel, bias, num_sites, num_hidden), tables,
                                     mu, seed, call_index, therm_steps, sweep_steps, samples_per_chain, configs_out,
                                     counters, st);
+}
+
+namespace vmc {
+__global__ void conj_kernel(const double2* __restrict__ g, int64_t n, double2* __restrict__ out) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = make_double2(g[i].x, -g[i].y);
+}
+
+__global__ void vjp_final_kernel(const double2* __restrict__ partial, int chunks, int L, int M, bool hasBias,
+                                 double2* __restrict__ out) {
+  const int rows = L + 1;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < (int64_t)rows * M;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int row = (int)(t / M);
+    if (row == 0 && !hasBias) continue;
+    double re = 0, im = 0;
+    for (int c = 0; c < chunks; ++c) {
+      const double2 a = partial[((size_t)c * 2 * rows) * M + t];
+      re += a.x;
+      im += a.y;
+    }
+    out[hasBias ? t : t - M] = make_double2(re, im);
+  }
+}
+}  // namespace vmc
+
+extern "C" size_t vmc_rbm_vjp_workspace_bytes(int64_t num_configs, int32_t num_sites, int32_t num_hidden) {
+  return vmc_rbm_grad_stats_workspace_bytes(num_configs, num_sites, num_hidden) + (size_t)num_configs * 16 + 256;
+}
+
+extern "C" int vmc_rbm_vjp(int32_t precision, const int32_t* configs, int64_t num_configs, int32_t num_sites,
+                           int32_t num_hidden, const void* kernel, const void* bias, const double* cotangent,
+                           double* out, void* workspace, size_t workspace_bytes, vmc_stream_t stream) {
+  int rc = check_rbm_args("vmc_rbm_vjp", precision, configs, num_configs, num_sites, num_hidden, kernel);
+  if (rc) return rc;
+  VMC_REQUIRE(num_configs > 0 && cotangent && out, VMC_ERR_INVALID_ARGUMENT, "vmc_rbm_vjp: null argument");
+  const size_t need = vmc_rbm_vjp_workspace_bytes(num_configs, num_sites, num_hidden);
+  VMC_REQUIRE(workspace && workspace_bytes >= need, VMC_ERR_WORKSPACE, "vmc_rbm_vjp: workspace of %zu bytes needed",
+              need);
+  unsigned char* ws = reinterpret_cast<unsigned char*>(workspace);
+  double2* tanhT = reinterpret_cast<double2*>(ws);
+  size_t off = ((size_t)num_configs * num_hidden * 16 + 255) & ~(size_t)255;
+  double2* partial = reinterpret_cast<double2*>(ws + off);
+  off += (((size_t)kStatChunks * 2 * (num_sites + 1) * (size_t)num_hidden * 16) + 255) & ~(size_t)255;
+  double2* csum = reinterpret_cast<double2*>(ws + off);
+  off += ((size_t)kStatChunks * 16 + 255) & ~(size_t)255;
+  double2* coef = reinterpret_cast<double2*>(ws + off);
+  cudaStream_t st = as_stream(stream);
+  const size_t el = precision == VMC_F64 ? 16 : 8;
+  size_t smem = (size_t)kWarpsPerBlock * (num_hidden * el + ((num_sites + 15) & ~15));
+  VMC_REQUIRE(smem <= 227 * 1024, VMC_ERR_UNSUPPORTED, "vmc_rbm_vjp: M=%d too large", num_hidden);
+  int grid = grid_for(num_configs);
+  if (precision == VMC_F64) {
+    set_smem((const void*)rbm_tanh_kernel<double>, smem);
+    rbm_tanh_kernel<double><<<grid, 32 * kWarpsPerBlock, smem, st>>>(
+        configs, num_configs, make_params<double>(kernel, bias, num_sites, num_hidden), tanhT);
+  } else {
+    set_smem((const void*)rbm_tanh_kernel<float>, smem);
+    rbm_tanh_kernel<float><<<grid, 32 * kWarpsPerBlock, smem, st>>>(
+        configs, num_configs, make_params<float>(kernel, bias, num_sites, num_hidden), tanhT);
+  }
+  rc = check_launch("vmc_rbm_vjp(tanh)");
+  if (rc) return rc;
+  conj_kernel<<<(int)std::min<int64_t>((num_configs + 255) / 256, 1024), 256, 0, st>>>(
+      reinterpret_cast<const double2*>(cotangent), num_configs, coef);
+  dim3 blk(32, kStatSiteGroups);
+  dim3 grd((num_hidden + 31) / 32, kStatChunks);
+  rbm_stats_partial_kernel<<<grd, blk, 0, st>>>(configs, tanhT, nullptr, nullptr, nullptr, num_configs, num_sites,
+                                                num_hidden, partial, csum, coef);
+  rc = check_launch("vmc_rbm_vjp(partial)");
+  if (rc) return rc;
+  int64_t outs = (int64_t)(num_sites + 1) * num_hidden;
+  vjp_final_kernel<<<(int)std::min<int64_t>((outs + 255) / 256, 152 * 4), 256, 0, st>>>(
+      partial, kStatChunks, num_sites, num_hidden, bias != nullptr, reinterpret_cast<double2*>(out));
+  return check_launch("vmc_rbm_vjp(final)");
 }

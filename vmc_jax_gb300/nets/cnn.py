@@ -3,6 +3,7 @@
 import numpy as np
 import torch
 
+from .. import _lib
 from . import activation_functions as act_funs
 
 
@@ -55,6 +56,7 @@ class CNN:
 
     def init(self, seed, sampleShape, device):
         """variance_scaling(1, fan_avg, uniform) kernels, zero biases (cnn.py:42,63-64)."""
+        self._shape = tuple(sampleShape)
         rng = np.random.default_rng(seed)
         params = {}
         for name, shape in self.leaf_shapes(sampleShape):
@@ -67,3 +69,61 @@ class CNN:
                 v = rng.uniform(-lim, lim, shape)
             params[name] = torch.as_tensor(v, dtype=torch.float64, device=device)
         return params
+
+    # ------------------------------------------------------------ kernels
+    @staticmethod
+    def _prec(precision):
+        return _lib.VMC_F32 if precision == "fp32" else _lib.VMC_F64
+
+    def desc(self, sampleShape):
+        """vmc_cnn_desc of this network on a lattice of shape ``sampleShape``."""
+        import ctypes
+        sampleShape = tuple(sampleShape)
+        if len(sampleShape) != len(self.F) or len(sampleShape) not in (1, 2):
+            raise NotImplementedError("CNN kernels support 1-D and 2-D lattices with matching filters")
+        if len(self.channels) > 4:
+            raise NotImplementedError("CNN kernels support up to 4 layers")
+        d = _CnnDesc()
+        d.ndim = len(sampleShape)
+        d.dims = (ctypes.c_int32 * 2)(*(list(sampleShape) + [1])[:2])
+        d.filter = (ctypes.c_int32 * 2)(*(list(self.F) + [1])[:2])
+        d.num_layers = len(self.channels)
+        d.channels = (ctypes.c_int32 * 4)(*(list(self.channels) + [0] * 4)[:4])
+        d.activation = (ctypes.c_int32 * 4)(*(self.act_codes + [0] * 4)[:4])
+        d.has_bias = (ctypes.c_int32 * 4)(*([int(self.layer_bias(l)) for l in range(len(self.channels))] + [0] * 4)[:4])
+        return d
+
+    def flat(self, params, precision):
+        dt = torch.float32 if precision == "fp32" else torch.float64
+        return torch.cat([p.reshape(-1) for p in params.values()]).to(dt).contiguous()
+
+    def logpsi(self, params, configs, precision="fp64", sampleShape=None):
+        N = configs.shape[0]
+        shape = sampleShape if sampleShape is not None else self._shape
+        out = torch.empty(N, dtype=torch.complex128, device=configs.device)
+        d = self.desc(shape)
+        _lib.call("vmc_cnn_logpsi", self._prec(precision), _lib.ctypes_ref(d), _lib.ptr(configs), N,
+                  _lib.ptr(self.flat(params, precision)), _lib.ptr(out), _lib.stream())
+        return out
+
+    def gradients(self, params, configs, precision="fp64", layout=_lib.VMC_GRAD_REFERENCE, sampleShape=None):
+        N = configs.shape[0]
+        shape = sampleShape if sampleShape is not None else self._shape
+        d = self.desc(shape)
+        P = sum(p.numel() for p in params.values())
+        if layout == _lib.VMC_GRAD_REFERENCE:
+            out = torch.empty((N, P), dtype=torch.complex128, device=configs.device)
+        else:
+            out = torch.empty((N, P), dtype=torch.float64, device=configs.device)
+        _lib.call("vmc_cnn_gradients", self._prec(precision), _lib.ctypes_ref(d), _lib.ptr(configs), N,
+                  _lib.ptr(self.flat(params, precision)), layout, _lib.ptr(out), _lib.stream())
+        return out
+
+
+import ctypes as _ct
+
+
+class _CnnDesc(_ct.Structure):
+    _fields_ = [("ndim", _ct.c_int32), ("dims", _ct.c_int32 * 2), ("filter", _ct.c_int32 * 2),
+                ("num_layers", _ct.c_int32), ("channels", _ct.c_int32 * 4), ("activation", _ct.c_int32 * 4),
+                ("has_bias", _ct.c_int32 * 4)]

@@ -72,8 +72,9 @@ class MCSampler:
         self.states = init.reshape(1, 1, -1).repeat(1, numChains, 1).contiguous()
         # make sure that net is initialised (sampler.py:124)
         self.net(self.states.reshape((1, numChains) + self.sampleShape))
-        if not isinstance(self.net.net, CpxRBM):
-            raise NotImplementedError("MCSampler has a CUDA kernel for CpxRBM states")
+        from .nets.cnn import CNN
+        if not isinstance(self.net.net, (CpxRBM, CNN)):
+            raise NotImplementedError("MCSampler has CUDA kernels for CpxRBM and CNN states")
         self.logProbFactor = logProbFactor
         self.mu = mu
         self.updateProposer = updateProposer
@@ -123,10 +124,21 @@ class MCSampler:
         return configs, logPsi, p.reshape(1, n)
 
     def _run_chains(self, psi, perChain):
+        from .nets.cnn import CNN
         params = psi.params_for()
         prec = psi.net._prec(psi.precision)
-        L, M = psi.net.dims(params)
         C = self.numChains
+        if isinstance(psi.net, CNN):
+            out = torch.empty((perChain * C, self.L), dtype=torch.int32, device=self.states.device)
+            self.counters.zero_()
+            d = psi.net.desc(self.sampleShape)
+            _lib.call("vmc_cnn_metropolis", prec, _lib.ctypes_ref(d), _lib.ptr(self.states), C,
+                      _lib.ptr(psi.net.flat(params, psi.precision)), float(self.mu), self.seed,
+                      self.callIndex & 0xFFFFFFFF, int(self.thermalizationSweeps * self.sweepSteps),
+                      int(self.sweepSteps), int(perChain), _lib.ptr(out), _lib.ptr(self.counters), _lib.stream())
+            self.callIndex += 1
+            return out.reshape((1, perChain * C) + self.sampleShape)
+        L, M = psi.net.dims(params)
         out = torch.empty((perChain * C, L), dtype=torch.int32, device=self.states.device)
         self.counters.zero_()
         _lib.call("vmc_rbm_metropolis", prec, _lib.ptr(self.states), C, L, M, _lib.ptr(params["kernel"]),
