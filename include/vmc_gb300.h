@@ -219,6 +219,23 @@ int vmc_rbm_grad_stats(int32_t precision, const int32_t* configs, int64_t num_co
                        const double* eloc, const double* eloc_mean, double* ok_mean, double* force,
                        void* workspace, size_t workspace_bytes, vmc_stream_t stream);
 
+/* vmc_rbm_grad_stats without a caller workspace, for callers that cannot
+ * allocate device memory at the point of the call (an XLA FFI handler, a
+ * runtime with a fixed memory budget, code inside a stream capture).  No
+ * counterpart in the reference: jVMC allocates through XLA.  The scratch is
+ * a 32 MiB static device array inside the library (held by every GPU that
+ * loads it until the process exits); problems needing more
+ * (vmc_rbm_grad_stats_workspace_bytes > 32 MiB) are rejected with
+ * VMC_ERR_UNSUPPORTED.  The first call on a device resolves the array's
+ * address (cudaGetSymbolAddress) and should come before any stream capture.
+ * All calls share the one array: calls that overlap on the GPU (different
+ * streams, or different host threads) race and must be serialised by the
+ * caller.  Results equal vmc_rbm_grad_stats's. */
+int vmc_rbm_grad_stats_noalloc(int32_t precision, const int32_t* configs, int64_t num_configs, int32_t num_sites,
+                               int32_t num_hidden, const void* kernel, const void* bias, const double* weights,
+                               const double* eloc, const double* eloc_mean, double* ok_mean, double* force,
+                               vmc_stream_t stream);
+
 /* ------------------------------------------------------------------------
  * Centred, weighted data of the S/F build and of the SNR transform
  * (stats.py:197-205, 255-292; tdvp.py:134-181) for a CpxRBM.

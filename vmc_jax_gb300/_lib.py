@@ -125,7 +125,7 @@ KERNELS_PER_CALL = {
     "vmc_rbm_grad_stats": 3, "vmc_rbm_centered_gradients": 1, "vmc_rbm_snr_data": 1, "vmc_gram_to_hermitian": 1,
     "vmc_zgemv": 1, "vmc_tdvp_snr": 1, "vmc_tdvp_regularize": 1, "vmc_gram_bf16x3": 1,
     "vmc_gemm_bf16x3_colsq": 1, "vmc_eigvec_bf16x2": 1, "vmc_cnn_logpsi": 1, "vmc_cnn_gradients": 1,
-    "vmc_cnn_metropolis": 1, "vmc_rbm_vjp": 4,
+    "vmc_cnn_metropolis": 1, "vmc_rbm_vjp": 4, "vmc_rbm_grad_stats_noalloc": 3,
 }
 launch_count = 0
 

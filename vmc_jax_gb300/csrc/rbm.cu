@@ -870,3 +870,63 @@ extern "C" int vmc_rbm_vjp(int32_t precision, const int32_t* configs, int64_t nu
       partial, kStatChunks, num_sites, num_hidden, bias != nullptr, reinterpret_cast<double2*>(out));
   return check_launch("vmc_rbm_vjp(final)");
 }
+
+// ===================================================================
+// Allocation-free variant of vmc_rbm_grad_stats.
+//
+// Some callers cannot call cudaMalloc at the point where they need the
+// statistics: a JAX/XLA FFI handler or an inference runtime that owns a
+// fixed memory budget, or code running while a stream is being captured
+// into a CUDA graph.  This entry point takes the scratch memory of
+// vmc_rbm_grad_stats from a file-scope device array instead of a caller
+// workspace.  The array (kNoAllocScratchBytes) is part of the library's
+// static device memory: every GPU that loads the library holds it until the
+// process exits.
+// ===================================================================
+namespace vmc {
+
+constexpr size_t kNoAllocScratchBytes = 32u << 20;  // 32 MiB per device
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+}  // namespace vmc
+
+#include <mutex>
+
+extern "C" int vmc_rbm_grad_stats_noalloc(int32_t precision, const int32_t* configs, int64_t num_configs,
+                                          int32_t num_sites, int32_t num_hidden, const void* kernel, const void* bias,
+                                          const double* weights, const double* eloc, const double* eloc_mean,
+                                          double* ok_mean, double* force, vmc_stream_t stream) {
+  int rc = check_rbm_args("vmc_rbm_grad_stats_noalloc", precision, configs, num_configs, num_sites, num_hidden,
+                          kernel);
+  if (rc) return rc;
+  const size_t need = vmc_rbm_grad_stats_workspace_bytes(num_configs, num_sites, num_hidden);
+  VMC_REQUIRE(need <= kNoAllocScratchBytes, VMC_ERR_UNSUPPORTED,
+              "vmc_rbm_grad_stats_noalloc: needs %zu bytes of scratch, the static scratch holds %zu "
+              "(num_configs * num_hidden * 16 + 1024 * (num_sites + 1) * num_hidden bytes must fit); use "
+              "vmc_rbm_grad_stats with a caller workspace",
+              need, kNoAllocScratchBytes);
+  // Device address of the scratch array, resolved once per device with that
+  // device current (host code sees only a stand-in for the symbol).
+  static std::mutex mu;
+  static void* addr[64] = {nullptr};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  VMC_REQUIRE(e == cudaSuccess && dev >= 0 && dev < 64, VMC_ERR_CUDA, "vmc_rbm_grad_stats_noalloc: %s",
+              cudaGetErrorString(e));
+  void* scratch;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    if (!addr[dev]) {
+      void* p = nullptr;
+      e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+      VMC_REQUIRE(e == cudaSuccess && p, VMC_ERR_CUDA, "vmc_rbm_grad_stats_noalloc: cudaGetSymbolAddress: %s",
+                  cudaGetErrorString(e));
+      addr[dev] = p;
+    }
+    scratch = addr[dev];
+  }
+  // Every buffer in the scratch is written before it is read (tanh values,
+  // per-chunk partial sums), so nothing has to start at zero.
+  return vmc_rbm_grad_stats(precision, configs, num_configs, num_sites, num_hidden, kernel, bias, weights, eloc,
+                            eloc_mean, ok_mean, force, scratch, kNoAllocScratchBytes, stream);
+}
