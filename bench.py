@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp32", "fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--kernel", default=None, choices=["gram", "snr", "eloc", "metropolis"],
+                    help="time one kernel on a fixed synthetic case instead of the TDVP step (profiling)")
     return ap.parse_args()
 
 
@@ -237,8 +239,83 @@ def run_reference(args):
           "phase_seconds": parts})
 
 
+def kernel_bench(args):
+    """One kernel on a fixed synthetic case, timed with CUDA events:
+    gram  tcgen05 BF16x3 Gram, rows 8192 x K 16384 (planes 537 MB > L2)
+    snr   tcgen05 BF16x3 colsq GEMM, 16384 x 8192 x 8192
+    eloc  fused E_loc of the L=64, M=256 Ising workload, 16384 samples
+    metropolis  RBM Metropolis, 1024 chains, L=64, M=256, 64 sweeps"""
+    import torch
+    import vmc_jax_gb300 as V
+    L_ = V._lib
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    st = L_.stream()
+    g = torch.Generator(device=dev).manual_seed(0)
+    if args.kernel in ("gram", "snr"):
+        if args.kernel == "gram":
+            rows, K = 8192, 16384
+            x = torch.randn(rows, K, device=dev, generator=g)
+            hi = x.to(torch.bfloat16)
+            lo = (x - hi.float()).to(torch.bfloat16)
+            del x
+            G = torch.empty((rows, rows), dtype=torch.float32, device=dev)
+            fn = lambda: L_.call("vmc_gram_bf16x3", L_.ptr(hi), L_.ptr(lo), rows, K, K, L_.ptr(G), rows, st)
+            alg = float(rows) * (rows + 1) * K
+            hw = 3.0 * rows * rows * K
+            shape = {"rows": rows, "k": K}
+        else:
+            m, n, K = 16384, 8192, 8192
+            a = torch.randn(m, K, device=dev, generator=g)
+            b = torch.randn(n, K, device=dev, generator=g) / 90.0
+            ah, bh = a.to(torch.bfloat16), b.to(torch.bfloat16)
+            al, bl = (a - ah.float()).to(torch.bfloat16), (b - bh.float()).to(torch.bfloat16)
+            del a, b
+            cs = torch.empty(n, dtype=torch.float32, device=dev)
+            fn = lambda: L_.call("vmc_gemm_bf16x3_colsq", L_.ptr(ah), L_.ptr(al), m, K, L_.ptr(bh), L_.ptr(bl), n, K,
+                                 K, L_.ptr(cs), st)
+            alg = 2.0 * m * n * K
+            hw = 3.0 * alg
+            shape = {"m": m, "n": n, "k": K}
+        unit, bound = "TFLOP/s", "tensor"
+    else:
+        cfg = WORKLOADS[DEFAULT_WORKLOAD]
+        ctx = build(cfg, "mixed")
+        psi, H = ctx["psi"], ctx["H"]
+        if args.kernel == "eloc":
+            s = torch.randint(0, 2, (1, 16384, cfg["L"]), dtype=torch.int32, device=dev, generator=g)
+            psi.rbm_tables()
+            fn = lambda: H.get_O_loc_fused(s, psi, None)
+            shape = {"samples": 16384, "L": cfg["L"], "M": cfg["M"], "strings": 2 * cfg["L"]}
+        else:
+            smp = ctx["sampler"]
+            fn = lambda: smp._run_chains(psi, 0)
+            smp.thermalizationSweeps = 64
+            shape = {"chains": cfg["chains"], "sweeps": 64, "L": cfg["L"], "M": cfg["M"]}
+        alg = hw = None
+        unit, bound = "ms", "latency/compute (FP32 + MUFU)"
+    for _ in range(max(args.warmup, 1)):
+        fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        fn()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    out = {"kernel": args.kernel, "ms_per_launch": ms, "shape": shape, "bound": bound}
+    if alg:
+        out["algorithmic_tflops"] = alg / ms / 1e9
+        out["executed_tflops"] = hw / ms / 1e9
+    emit(out)
+
+
 def main():
     args = parse()
+    if args.kernel:
+        kernel_bench(args)
+        return
     if args.impl == "reference":
         run_reference(args)
         return
