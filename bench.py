@@ -51,6 +51,11 @@ def parse():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp32", "fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--serve", action="store_true",
+                    help="serving load: Poisson stream of independent Ising jobs through vmc_jax_gb300.serving")
+    ap.add_argument("--jobs", type=int, default=16)
+    ap.add_argument("--rate", type=float, default=2.0, help="job arrivals per second (--serve)")
+    ap.add_argument("--job-steps", type=int, default=10)
     ap.add_argument("--kernel", default=None, choices=["gram", "snr", "eloc", "metropolis"],
                     help="time one kernel on a fixed synthetic case instead of the TDVP step (profiling)")
     return ap.parse_args()
@@ -311,8 +316,44 @@ def kernel_bench(args):
     emit(out)
 
 
+def serve_bench(args):
+    """Poisson arrivals of independent jobs (L in {16, 24, 32}, h ~ U[0.5, 1.5],
+    M in {1, 2} L, N_s in {2^11, 2^12, 2^13}, ground-state or quench) served by
+    the continuous-batching loop; p50/p99 per-step and per-job latency."""
+    import torch
+    from vmc_jax_gb300.serving import JobSpec, Server
+    torch.cuda.set_device(0)
+    rng = np.random.default_rng(123)
+    t = 0.0
+    specs = []
+    for j in range(args.jobs):
+        t += rng.exponential(1.0 / args.rate)
+        L = int(rng.choice([16, 24, 32]))
+        specs.append(JobSpec(L=L, h=float(rng.uniform(0.5, 1.5)), M=int(rng.choice([1, 2])) * L,
+                             num_samples=int(2 ** rng.integers(11, 14)), steps=args.job_steps, seed=j,
+                             kind="quench" if j % 4 == 3 else "ground_state",
+                             dt=0.005 if j % 4 == 3 else 0.01, arrival=t, precision=args.precision))
+    # warm-up: one small job compiles nothing but pages in the libraries
+    w = Server(max_slots=1)
+    w.submit(JobSpec(L=8, h=1.0, M=8, num_samples=256, steps=2))
+    w.run()
+    srv = Server(max_slots=8)
+    for sp in specs:
+        srv.submit(sp)
+    rep = srv.run()
+    emit({"metric": "served TDVP steps/s and p50/p99 latency", "value": rep["steps_per_s"], "unit": "steps/s",
+          "n_gpus": 1, "higher_is_better": True, "data": "synthetic (seeded job stream)",
+          "config": {"workload": "poisson_ising_jobs", "jobs": args.jobs, "rate_per_s": args.rate,
+                     "steps_per_job": args.job_steps, "L": [16, 24, 32], "M_over_L": [1, 2],
+                     "N_s": [2048, 4096, 8192], "precision": args.precision},
+          **rep})
+
+
 def main():
     args = parse()
+    if args.serve:
+        serve_bench(args)
+        return
     if args.kernel:
         kernel_bench(args)
         return

@@ -128,6 +128,16 @@ int vmc_rbm_metropolis(int32_t precision, int32_t* states, int32_t num_chains, i
 int vmc_metropolis_draws_host(uint64_t seed, uint32_t call_index, uint32_t step, int32_t num_chains,
                               int32_t num_sites, int32_t* sites, double* uniforms);
 
+/* vmc_rbm_metropolis with the call index read from device memory
+ * (*call_index, uint32) and incremented after the sweep on the same stream:
+ * a CUDA graph that captures it draws a fresh random stream on every replay
+ * (the serving loop's shared graph launches). */
+int vmc_rbm_metropolis_devcall(int32_t precision, int32_t* states, int32_t num_chains, int32_t num_sites,
+                               int32_t num_hidden, const void* kernel, const void* bias, const void* tables,
+                               double mu, uint64_t seed, uint32_t* call_index, int64_t therm_steps,
+                               int64_t sweep_steps, int64_t samples_per_chain, int32_t* configs_out, void* counters,
+                               vmc_stream_t stream);
+
 /* Metropolis weights p_r = exp(factor * Re log_psi_r) / sum (sampler.py:234-235,
  * factor = 1/logProbFactor - mu).  workspace: vmc_reduce_workspace_bytes(1). */
 int vmc_mc_probabilities(const double* log_psi, int64_t num_samples, double factor, double* p, void* workspace,

@@ -126,6 +126,7 @@ KERNELS_PER_CALL = {
     "vmc_zgemv": 1, "vmc_tdvp_snr": 1, "vmc_tdvp_regularize": 1, "vmc_gram_bf16x3": 1,
     "vmc_gemm_bf16x3_colsq": 1, "vmc_eigvec_bf16x2": 1, "vmc_cnn_logpsi": 1, "vmc_cnn_gradients": 1,
     "vmc_cnn_metropolis": 1, "vmc_rbm_vjp": 4, "vmc_rbm_grad_stats_noalloc": 3,
+    "vmc_rbm_metropolis_devcall": 2,
 }
 launch_count = 0
 
@@ -178,8 +179,10 @@ class Workspace:
 
     @classmethod
     def get(cls, nbytes, device=None):
+        """Scratch of at least nbytes for the calling thread on ``device``
+        (one buffer per host thread, so concurrent solvers never share)."""
         device = torch.device("cuda", torch.cuda.current_device()) if device is None else device
-        key = (device.index, "main")
+        key = (device.index, threading.get_ident())
         buf = cls._bufs.get(key)
         if buf is None or buf.numel() < nbytes:
             buf = torch.empty(max(int(nbytes), 1 << 20), dtype=torch.uint8, device=device)

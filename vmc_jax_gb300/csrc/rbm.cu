@@ -628,12 +628,13 @@ namespace vmc {
 template <typename T, int JPL>
 __global__ void __launch_bounds__(256) rbm_metropolis_kernel(
     int32_t* __restrict__ states, int C, rbm_params<T> p, const cpx<T>* __restrict__ tab, double mu, uint64_t seed,
-    uint32_t call, int64_t thermSteps, int64_t sweepSteps, int64_t samplesPerChain, int32_t* __restrict__ configsOut,
-    unsigned long long* __restrict__ counters) {
+    uint32_t callArg, const uint32_t* __restrict__ callPtr, int64_t thermSteps, int64_t sweepSteps,
+    int64_t samplesPerChain, int32_t* __restrict__ configsOut, unsigned long long* __restrict__ counters) {
   extern __shared__ unsigned char smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int chain = blockIdx.x * (blockDim.x >> 5) + warp;
   if (chain >= C) return;  // whole warps exit together
+  const uint32_t call = callPtr ? *callPtr : callArg;
   const int L = p.L, M = p.M;
   int8_t* cfg = reinterpret_cast<int8_t*>(smem) + warp * ((L + 15) & ~15);
   int32_t* st = states + (size_t)chain * L;
@@ -746,28 +747,34 @@ __global__ void __launch_bounds__(256) rbm_metropolis_kernel(
 
 template <typename T, int JPL>
 int launch_metropolis(int32_t* states, int C, rbm_params<T> p, const void* tables, double mu, uint64_t seed,
-                      uint32_t call, int64_t therm, int64_t sweep, int64_t spc, int32_t* out, void* counters,
-                      cudaStream_t st) {
+                      uint32_t call, const uint32_t* callPtr, int64_t therm, int64_t sweep, int64_t spc,
+                      int32_t* out, void* counters, cudaStream_t st) {
   const int warps = 4;
   const size_t smem = (size_t)warps * ((p.L + 15) & ~15);
   const int grid = (C + warps - 1) / warps;
   rbm_metropolis_kernel<T, JPL><<<grid, 32 * warps, smem, st>>>(
-      states, C, p, reinterpret_cast<const cpx<T>*>(tables), mu, seed, call, therm, sweep, spc, out,
+      states, C, p, reinterpret_cast<const cpx<T>*>(tables), mu, seed, call, callPtr, therm, sweep, spc, out,
       reinterpret_cast<unsigned long long*>(counters));
   return check_launch("vmc_rbm_metropolis");
 }
 
 template <typename T>
 int dispatch_metropolis(int32_t* states, int C, rbm_params<T> p, const void* tables, double mu, uint64_t seed,
-                        uint32_t call, int64_t therm, int64_t sweep, int64_t spc, int32_t* out, void* counters,
-                        cudaStream_t st) {
+                        uint32_t call, const uint32_t* cp, int64_t therm, int64_t sweep, int64_t spc, int32_t* out,
+                        void* counters, cudaStream_t st) {
   const int jpl = (p.M + 31) / 32;
-  if (jpl <= 1) return launch_metropolis<T, 1>(states, C, p, tables, mu, seed, call, therm, sweep, spc, out, counters, st);
-  if (jpl <= 2) return launch_metropolis<T, 2>(states, C, p, tables, mu, seed, call, therm, sweep, spc, out, counters, st);
-  if (jpl <= 4) return launch_metropolis<T, 4>(states, C, p, tables, mu, seed, call, therm, sweep, spc, out, counters, st);
-  if (jpl <= 8) return launch_metropolis<T, 8>(states, C, p, tables, mu, seed, call, therm, sweep, spc, out, counters, st);
-  if (jpl <= 16) return launch_metropolis<T, 16>(states, C, p, tables, mu, seed, call, therm, sweep, spc, out, counters, st);
-  return launch_metropolis<T, 32>(states, C, p, tables, mu, seed, call, therm, sweep, spc, out, counters, st);
+  if (jpl <= 1) return launch_metropolis<T, 1>(states, C, p, tables, mu, seed, call, cp, therm, sweep, spc, out, counters, st);
+  if (jpl <= 2) return launch_metropolis<T, 2>(states, C, p, tables, mu, seed, call, cp, therm, sweep, spc, out, counters, st);
+  if (jpl <= 4) return launch_metropolis<T, 4>(states, C, p, tables, mu, seed, call, cp, therm, sweep, spc, out, counters, st);
+  if (jpl <= 8) return launch_metropolis<T, 8>(states, C, p, tables, mu, seed, call, cp, therm, sweep, spc, out, counters, st);
+  if (jpl <= 16) return launch_metropolis<T, 16>(states, C, p, tables, mu, seed, call, cp, therm, sweep, spc, out, counters, st);
+  return launch_metropolis<T, 32>(states, C, p, tables, mu, seed, call, cp, therm, sweep, spc, out, counters, st);
+}
+
+// call index read from device memory and advanced by the same stream:
+// replaying a captured graph draws fresh random numbers every time
+__global__ void counter_add_kernel(uint32_t* c, uint32_t v) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *c += v;
 }
 
 }  // namespace vmc
@@ -789,11 +796,39 @@ extern "C" int vmc_rbm_metropolis(int32_t precision, int32_t* states, int32_t nu
   cudaStream_t st = as_stream(stream);
   if (precision == VMC_F64)
     return dispatch_metropolis<double>(states, num_chains, make_params<double>(kernel, bias, num_sites, num_hidden),
-                                       tables, mu, seed, call_index, therm_steps, sweep_steps, samples_per_chain,
-                                       configs_out, counters, st);
+                                       tables, mu, seed, call_index, nullptr, therm_steps, sweep_steps,
+                                       samples_per_chain, configs_out, counters, st);
   return dispatch_metropolis<float>(states, num_chains, make_params<float>(kernel, bias, num_sites, num_hidden), tables,
-                                    mu, seed, call_index, therm_steps, sweep_steps, samples_per_chain, configs_out,
+                                    mu, seed, call_index, nullptr, therm_steps, sweep_steps, samples_per_chain,
+                                    configs_out, counters, st);
+}
+
+extern "C" int vmc_rbm_metropolis_devcall(int32_t precision, int32_t* states, int32_t num_chains, int32_t num_sites,
+                                          int32_t num_hidden, const void* kernel, const void* bias,
+                                          const void* tables, double mu, uint64_t seed, uint32_t* call_index,
+                                          int64_t therm_steps, int64_t sweep_steps, int64_t samples_per_chain,
+                                          int32_t* configs_out, void* counters, vmc_stream_t stream) {
+  int rc = check_rbm_args("vmc_rbm_metropolis_devcall", precision, states, num_chains, num_sites, num_hidden, kernel);
+  if (rc) return rc;
+  VMC_REQUIRE(num_hidden <= 1024, VMC_ERR_UNSUPPORTED, "vmc_rbm_metropolis_devcall: M=%d > 1024", num_hidden);
+  VMC_REQUIRE(num_chains > 0 && tables && counters && call_index && sweep_steps > 0 && therm_steps >= 0 &&
+                  samples_per_chain >= 0 && (configs_out || samples_per_chain == 0),
+              VMC_ERR_INVALID_ARGUMENT, "vmc_rbm_metropolis_devcall: bad arguments");
+  VMC_REQUIRE(therm_steps + sweep_steps * samples_per_chain < (int64_t)0xFFFFFFFF, VMC_ERR_UNSUPPORTED,
+              "vmc_rbm_metropolis_devcall: more than 2^32 steps in one call");
+  VMC_REQUIRE(mu >= 0.0 && mu <= 2.0, VMC_ERR_INVALID_ARGUMENT, "vmc_rbm_metropolis_devcall: mu=%g", mu);
+  cudaStream_t st = as_stream(stream);
+  if (precision == VMC_F64)
+    rc = dispatch_metropolis<double>(states, num_chains, make_params<double>(kernel, bias, num_sites, num_hidden),
+                                     tables, mu, seed, 0u, call_index, therm_steps, sweep_steps, samples_per_chain,
+                                     configs_out, counters, st);
+  else
+    rc = dispatch_metropolis<float>(states, num_chains, make_params<float>(kernel, bias, num_sites, num_hidden), tables,
+                                    mu, seed, 0u, call_index, therm_steps, sweep_steps, samples_per_chain, configs_out,
                                     counters, st);
+  if (rc) return rc;
+  counter_add_kernel<<<1, 32, 0, st>>>(call_index, 1u);
+  return check_launch("vmc_rbm_metropolis_devcall(counter)");
 }
 
 namespace vmc {

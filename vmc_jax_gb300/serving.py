@@ -1,0 +1,323 @@
+"""Continuous-batching server for independent TDVP jobs on one GPU.
+
+A job is a transverse-field Ising chain (L sites, couplings J and h) with a
+CpxRBM of M hidden units, N_s Monte Carlo samples per step and a number of
+TDVP steps: either an imaginary-time ground-state search (makeReal='real',
+x = 1) or a real-time quench (makeReal='imag', x = i), Euler-integrated.
+
+* Jobs arrive at any time (``submit``).  A job is admitted when a slot is
+  free and its estimated HBM footprint fits the budget; until then it waits.
+* An admitted job's parameters, Markov chains, random-stream counter and
+  integrator state stay on the device in persistent per-slot buffers.
+* Each tick launches the sampling + E_loc phase of every job that is ready
+  for its next step as ONE CUDA graph (each job's kernels on its own branch;
+  the graph is captured once per set of ready jobs and replayed), then each
+  job's FP64 solve runs on its own stream from its own host thread, so the
+  solves of different jobs overlap on the GPU, and the next tick samples
+  whichever jobs are ready again.
+* Per-step latency (graph launch to update applied) and per-job latency
+  (arrival to last step) are recorded for p50/p99 reporting.
+
+A job computes exactly what it computes alone: its kernels, inputs and
+random stream do not depend on the other jobs; only the FP32 atomic column
+sums of the SNR contraction can round differently run to run.
+"""
+
+import dataclasses
+import math
+import threading
+import time
+
+import numpy as np
+import torch
+
+from . import _lib
+from . import global_defs
+from . import mpi_wrapper as mpi
+from .nets.rbm import CpxRBM
+from .operator.branch_free import BranchFreeOperator, Sx, Sz, scal_opstr
+from .sampler import MCSampler, propose_spin_flip
+from .util.tdvp import TDVP
+from .vqs import NQS
+
+
+@dataclasses.dataclass
+class JobSpec:
+    L: int
+    h: float
+    M: int
+    num_samples: int
+    steps: int = 50
+    kind: str = "ground_state"   # or "quench"
+    J: float = 1.0
+    dt: float = 0.01
+    seed: int = 0
+    chains: int = 0              # 0: min(1024, num_samples // 4)
+    precision: str = "mixed"
+    arrival: float = 0.0         # seconds after the server starts
+
+    @property
+    def num_params(self):
+        return self.L * self.M + self.M
+
+    def num_chains(self):
+        return self.chains or max(1, min(1024, self.num_samples // 4))
+
+
+def footprint_bytes(spec):
+    """Conservative HBM estimate of one job's step (all buffers of the mixed
+    pipeline alive at once)."""
+    P, N, L = spec.num_params, spec.num_samples, spec.L
+    P2 = 2 * P
+    b = 0
+    b += 2 * P2 * N * 2          # centred O_k planes (bf16 hi/lo)
+    b += P2 * P2 * 4             # FP32 Gram
+    b += 4 * P * P * 16          # A, eigenvectors, eigh workspace (estimate)
+    b += 2 * N * P2 * 2          # SNR data planes
+    b += 2 * P2 * P2 * 2         # eigenvector planes
+    b += N * L * 4 * 2 + N * 64  # configs, per-sample scalars
+    b += 64 << 20                # statistics workspace, tables, slack
+    return b
+
+
+def percentile(x, q):
+    if not x:
+        return None
+    return float(np.percentile(np.asarray(x), q))
+
+
+class _Slot:
+    """Device-resident state of one admitted job."""
+
+    def __init__(self, job_id, spec, arrival_wall):
+        self.id = job_id
+        self.spec = spec
+        self.arrival_wall = arrival_wall
+        self.steps_done = 0
+        self.step_latencies = []
+        self.energies = []
+        self.stream = torch.cuda.Stream()
+        L, M = spec.L, spec.M
+        dev = global_defs.device()
+        rng = np.random.default_rng(spec.seed)
+        theta = np.concatenate([rng.normal(0, 0.01, M), rng.normal(0, 0.01, M),
+                                rng.normal(0, 0.01, L * M), rng.normal(0, 0.01, L * M)])
+        if spec.kind == "quench":
+            theta = theta * 20.0
+        self.psi = NQS(CpxRBM(numHidden=M, bias=True), precision="fp64" if spec.precision == "fp64" else "fp32")
+        self.psi(np.zeros((1, 1, L), np.int32))
+        self.psi.set_parameters(theta)
+        self.H = BranchFreeOperator()
+        for l in range(L):
+            self.H.add(scal_opstr(-spec.J, (Sz(l), Sz((l + 1) % L))))
+            self.H.add(scal_opstr(-spec.h, (Sx(l),)))
+        C = spec.num_chains()
+        self.sampler = MCSampler(self.psi, (L,), spec.seed, updateProposer=propose_spin_flip, numChains=C,
+                                 numSamples=spec.num_samples, thermalizationSweeps=8, sweepSteps=L)
+        if spec.kind == "quench":
+            self.tdvp = TDVP(self.sampler, makeReal="imag", rhsPrefactor=1.j, pinvCutoff=1e-8,
+                             precision=spec.precision)
+        else:
+            self.tdvp = TDVP(self.sampler, makeReal="real", rhsPrefactor=1., pinvCutoff=1e-8,
+                             precision=spec.precision)
+        # persistent buffers read by the captured sampling / E_loc graph
+        self.kprec = "fp64" if spec.precision == "fp64" else "fp32"
+        pr = self.psi.params_for(self.kprec)
+        self.W = pr["kernel"].clone().contiguous()
+        self.b = pr["bias"].clone().contiguous()
+        self.tables = self.psi.net.tables({"kernel": self.W}, self.kprec).clone()
+        self.perChain = int(math.ceil(spec.num_samples / C))
+        self.N = self.perChain * C
+        self.configs = torch.empty((self.N, L), dtype=torch.int32, device=dev)
+        self.logpsi = torch.empty(self.N, dtype=torch.complex128, device=dev)
+        self.p = torch.empty(self.N, dtype=torch.float64, device=dev)
+        self.eloc = torch.empty(self.N, dtype=torch.complex128, device=dev)
+        self.ws = torch.empty(_lib.query("vmc_reduce_workspace_bytes", 1), dtype=torch.uint8, device=dev)
+        self.call = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.counters = torch.zeros(2, dtype=torch.int64, device=dev)
+        self.op = self.H._device_operator()
+        self.sampler.globNumSamples = self.N
+        self.theta = self.psi.get_parameters()
+
+    # ---- phase 1: captured into the shared graph
+    def launch_sampling(self):
+        spec = self.spec
+        prec = CpxRBM._prec(self.kprec)
+        L, M, C = spec.L, spec.M, self.sampler.numChains
+        st = _lib.stream()
+        _lib.call("vmc_rbm_prepare", prec, L, M, _lib.ptr(self.W), _lib.ptr(self.tables), st)
+        _lib.call("vmc_rbm_metropolis_devcall", prec, _lib.ptr(self.sampler.states), C, L, M, _lib.ptr(self.W),
+                  _lib.ptr(self.b), _lib.ptr(self.tables), float(self.sampler.mu), self.sampler.seed,
+                  _lib.ptr(self.call), int(self.sampler.thermalizationSweeps * self.sampler.sweepSteps),
+                  int(self.sampler.sweepSteps), self.perChain, _lib.ptr(self.configs), _lib.ptr(self.counters), st)
+        _lib.call("vmc_rbm_logpsi", prec, _lib.ptr(self.configs), self.N, L, M, _lib.ptr(self.W), _lib.ptr(self.b),
+                  _lib.ptr(self.logpsi), st)
+        _lib.call("vmc_mc_probabilities", _lib.ptr(self.logpsi), self.N,
+                  float(1.0 / self.sampler.logProbFactor - self.sampler.mu), _lib.ptr(self.p), _lib.ptr(self.ws),
+                  self.ws.numel(), st)
+        _lib.call("vmc_rbm_oloc_fused", prec, _lib.ptr(self.configs), self.N, L, M, _lib.ptr(self.W),
+                  _lib.ptr(self.b), _lib.ptr(self.tables), self.op, None, _lib.ptr(self.eloc), st)
+
+    # ---- phase 2: the job's own stream and host thread
+    def solve(self, ready_event, t_launch):
+        with torch.cuda.stream(self.stream):
+            self.stream.wait_event(ready_event)
+            configs = self.configs.reshape(1, self.N, self.spec.L)
+            update, _, _ = self.tdvp._rbm_rhs(self.psi, configs, self.eloc.reshape(1, -1), self.p.reshape(1, -1))
+            self.energies.append(self.tdvp.ElocMean.real.clone())
+            self.theta = self.theta + self.spec.dt * update
+            self.psi.set_parameters(self.theta)
+            pr = self.psi.params_for(self.kprec)
+            self.W.copy_(pr["kernel"])
+            self.b.copy_(pr["bias"])
+            self.stream.synchronize()
+        self.steps_done += 1
+        self.step_latencies.append(time.perf_counter() - t_launch)
+
+    @property
+    def finished(self):
+        return self.steps_done >= self.spec.steps
+
+
+class Server:
+    """Persistent request loop over one GPU (see the module docstring).
+
+    ``hbm_budget``: bytes the admitted jobs' footprints may sum to (default:
+    80% of the free device memory); ``max_slots``: jobs resident at once;
+    ``batch_window``: seconds a tick waits for more jobs to become ready."""
+
+    def __init__(self, hbm_budget=None, max_slots=8, batch_window=0.002):
+        _lib.require_cuda()
+        if hbm_budget is None:
+            free, _ = torch.cuda.mem_get_info()
+            hbm_budget = int(0.8 * free)
+        self.hbm_budget = hbm_budget
+        self.max_slots = max_slots
+        self.batch_window = batch_window
+        self.queue = []
+        self.active = {}
+        self.done = {}
+        self.graphs = {}
+        self.lock = threading.Condition()
+        self.ready = set()
+        self.next_id = 0
+        self.t0 = None
+        self.sample_stream = torch.cuda.Stream()
+        self.max_resident = 0
+        self.graph_launches = 0
+
+    def submit(self, spec):
+        with self.lock:
+            jid = self.next_id
+            self.next_id += 1
+            self.queue.append((jid, spec))
+            self.lock.notify_all()
+            return jid
+
+    def _used(self):
+        return sum(footprint_bytes(s.spec) for s in self.active.values())
+
+    def _admit(self, now):
+        admitted = []
+        for item in list(self.queue):
+            jid, spec = item
+            if spec.arrival > now:
+                continue
+            if len(self.active) >= self.max_slots:
+                break
+            if self._used() + footprint_bytes(spec) > self.hbm_budget:
+                if not self.active:
+                    raise RuntimeError("job %d needs %.1f GB, more than the HBM budget"
+                                       % (jid, footprint_bytes(spec) / 1e9))
+                continue
+            self.queue.remove(item)
+            slot = _Slot(jid, spec, self.t0 + spec.arrival)
+            self.active[jid] = slot
+            self.ready.add(jid)
+            admitted.append(jid)
+        self.max_resident = max(self.max_resident, len(self.active))
+        return admitted
+
+    def _graph_for(self, ids):
+        key = tuple(sorted(ids))
+        g = self.graphs.get(key)
+        if g is None:
+            torch.cuda.synchronize()
+            g = torch.cuda.CUDAGraph()
+            cap = self.sample_stream
+            with torch.cuda.graph(g, stream=cap, capture_error_mode="thread_local"):
+                branches = []
+                for jid in key:
+                    br = self.active[jid].stream
+                    br.wait_stream(cap)
+                    with torch.cuda.stream(br):
+                        self.active[jid].counters.zero_()
+                        self.active[jid].launch_sampling()
+                    branches.append(br)
+                for br in branches:
+                    cap.wait_stream(br)
+            self.graphs[key] = g
+        return g
+
+    def run(self):
+        """Serve until every submitted job has finished; returns the report."""
+        self.t0 = time.perf_counter()
+        workers = {}
+        while True:
+            with self.lock:
+                now = time.perf_counter() - self.t0
+                self._admit(now)
+                if not self.queue and not self.active:
+                    break
+                if not self.ready:
+                    # wait for a solve to finish or the next arrival
+                    nxt = min([s.arrival for _, s in self.queue], default=None)
+                    timeout = 0.05 if nxt is None else max(1e-4, min(0.05, nxt - now))
+                    self.lock.wait(timeout)
+                    continue
+            time.sleep(self.batch_window)  # let more jobs become ready
+            with self.lock:
+                ids = sorted(self.ready)
+                self.ready.clear()
+                self.graphs = {k: v for k, v in self.graphs.items() if all(i in self.active for i in k)}
+            g = self._graph_for(ids)
+            t_launch = time.perf_counter()
+            with torch.cuda.stream(self.sample_stream):
+                g.replay()
+                ev = torch.cuda.Event()
+                ev.record(self.sample_stream)
+            self.graph_launches += 1
+            for jid in ids:
+                slot = self.active[jid]
+                th = threading.Thread(target=self._work, args=(slot, ev, t_launch), daemon=True)
+                workers[jid] = th
+                th.start()
+        for th in workers.values():
+            th.join()
+        return self.report()
+
+    def _work(self, slot, ev, t_launch):
+        slot.solve(ev, t_launch)
+        with self.lock:
+            if slot.finished:
+                slot.job_latency = time.perf_counter() - slot.arrival_wall
+                self.done[slot.id] = slot
+                del self.active[slot.id]
+            else:
+                self.ready.add(slot.id)
+            self.lock.notify_all()
+
+    def report(self):
+        steps = [x for s in self.done.values() for x in s.step_latencies]
+        jobs = [s.job_latency for s in self.done.values()]
+        wall = time.perf_counter() - self.t0
+        return {"jobs": len(self.done), "steps": len(steps), "wall_s": wall,
+                "steps_per_s": len(steps) / wall if wall > 0 else None,
+                "step_latency_s": {"p50": percentile(steps, 50), "p99": percentile(steps, 99)},
+                "job_latency_s": {"p50": percentile(jobs, 50), "p99": percentile(jobs, 99)},
+                "max_resident_jobs": self.max_resident, "graph_launches": self.graph_launches}
+
+    def result(self, job_id):
+        """Final flat parameters and per-step energies of a finished job."""
+        s = self.done[job_id]
+        return s.theta, torch.stack(s.energies)

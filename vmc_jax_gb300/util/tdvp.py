@@ -238,9 +238,18 @@ class TDVP:
             del Y
             realRep, cprec = 0, _lib.VMC_F64
         self.rhoVar_c = torch.empty(P, dtype=torch.float64, device=dev)
-        _lib.call("vmc_tdvp_snr", _lib.ptr(vtf), cprec, _lib.ptr(colsq), P, realRep, float(mpi.globNumSamples),
+        _lib.call("vmc_tdvp_snr", _lib.ptr(vtf), cprec, _lib.ptr(colsq), P, realRep, float(self._num_samples()),
                   _lib.ptr(snr), _lib.ptr(self.rhoVar_c), st)
         return snr
+
+    def _num_samples(self):
+        """The global sample count of the last sampling call (mpi.globNumSamples,
+        tdvp.py:179), taken from this solver's sampler so that solvers of
+        different jobs can run concurrently."""
+        n = getattr(self.sampler, "globNumSamples", None)
+        if isinstance(self.sampler, ExactSampler) or not n:
+            return mpi.globNumSamples
+        return n
 
     def _rbm_metadata(self, psi, update, residual, cutoff):
         """tdvp_error (tdvp.py:102-104) and the 2P spectrum / SNR."""
