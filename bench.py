@@ -37,6 +37,8 @@ WORKLOADS = {
     "ising64_rbm256_mcmc16k": dict(L=64, M=256, J=1.0, h=1.0, chains=1024, therm=64, per_chain=16, dt=0.01,
                                    sampler="mc"),
     "ising10_rbm20_exact": dict(L=10, M=20, J=1.0, h=0.7, dt=0.01, sampler="exact"),
+    "ising10x10_cnn8x8_mcmc32k": dict(Lx=10, Ly=10, J=1.0, h=3.0, chains=4096, therm=10, per_chain=8, dt=0.01,
+                                       sampler="mc", net="cnn"),
 }
 DEFAULT_WORKLOAD = "ising64_rbm256_mcmc16k"
 
@@ -56,6 +58,9 @@ def parse():
     ap.add_argument("--jobs", type=int, default=16)
     ap.add_argument("--rate", type=float, default=2.0, help="job arrivals per second (--serve)")
     ap.add_argument("--job-steps", type=int, default=10)
+    ap.add_argument("--quench", type=float, default=None,
+                    help="XXZ L=48 real-time quench with the adaptive Heun integrator up to this time: energy drift "
+                         "of the mixed form and of the FP64 form")
     ap.add_argument("--kernel", default=None, choices=["gram", "snr", "eloc", "metropolis"],
                     help="time one kernel on a fixed synthetic case instead of the TDVP step (profiling)")
     return ap.parse_args()
@@ -75,8 +80,44 @@ def initial_parameters(cfg):
     return np.concatenate([b.real, b.imag, W.real.ravel(), W.imag.ravel()])
 
 
+def build_cnn(cfg, precision):
+    """10x10 TFIM with a real CNN (3x3 filters, 8 and 8 channels, x^2/2 - x^4/12,
+    bias on the second layer), He-normal parameters from seed 0, MCSampler."""
+    import vmc_jax_gb300 as V
+    Lx, Ly = cfg["Lx"], cfg["Ly"]
+    net = V.nets.CNN(F=(3, 3), channels=(8, 8), strides=(1, 1), actFun=(V.nets.activation_functions.poly4,))
+    psi = V.vqs.NQS(net, precision="fp64" if precision == "fp64" else "fp32")
+    psi(np.zeros((1, 1, Lx, Ly), np.int32))
+    rng = np.random.default_rng(0)
+    theta = []
+    for name, shape in net.leaf_shapes((Lx, Ly)):
+        if name.endswith("bias"):
+            theta.append(np.zeros(shape).ravel())
+        else:
+            fan_in = int(np.prod(shape[:-1]))
+            theta.append(rng.normal(0, np.sqrt(2.0 / fan_in), shape).ravel())
+    psi.set_parameters(np.concatenate(theta))
+    H = V.operator.BranchFreeOperator()
+    for y in range(Ly):
+        for x in range(Lx):
+            i = y * Lx + x
+            H.add(V.operator.scal_opstr(-cfg["J"], (V.operator.Sz(i), V.operator.Sz(y * Lx + (x + 1) % Lx))))
+            H.add(V.operator.scal_opstr(-cfg["J"], (V.operator.Sz(i), V.operator.Sz(((y + 1) % Ly) * Lx + x))))
+            H.add(V.operator.scal_opstr(-cfg["h"], (V.operator.Sx(i),)))
+    ns = cfg["chains"] * cfg["per_chain"]
+    sampler = V.sampler.MCSampler(psi, (Lx, Ly), 0, updateProposer=V.sampler.propose_spin_flip,
+                                  numChains=cfg["chains"], numSamples=ns, thermalizationSweeps=cfg["therm"],
+                                  sweepSteps=Lx * Ly)
+    tdvp = V.util.TDVP(sampler, makeReal="real", rhsPrefactor=1., pinvCutoff=1e-8, snrTol=2, precision=precision)
+    stepper = V.util.stepper.Euler(timeStep=cfg["dt"])
+    P = sum(int(np.prod(sh)) for _, sh in net.leaf_shapes((Lx, Ly)))
+    return dict(V=V, psi=psi, H=H, sampler=sampler, tdvp=tdvp, stepper=stepper, ns=ns, P=P)
+
+
 def build(cfg, precision):
     import vmc_jax_gb300 as V
+    if cfg.get("net") == "cnn":
+        return build_cnn(cfg, precision)
     L, M = cfg["L"], cfg["M"]
     psi = V.vqs.NQS(V.nets.CpxRBM(numHidden=M, bias=True), precision="fp64" if precision == "fp64" else "fp32")
     psi(np.zeros((1, 1, L), np.int32))
@@ -161,6 +202,8 @@ def cpu_step_seconds(cfg, budget_note):
     and SNR contraction by N_s * n^2 (GEMM rate at a smaller n), the 2P
     eigendecomposition by n^3 (LAPACK at a smaller n)."""
     from oracle import jvmc_oracle as O
+    if cfg.get("net") == "cnn":
+        return cnn_cpu_step_seconds(cfg)
     L, M = cfg["L"], cfg["M"]
     rng = np.random.default_rng(0)
     prm = O.init_cpx_rbm(L, M, True, rng, scale=0.01)
@@ -204,12 +247,73 @@ def cpu_step_seconds(cfg, budget_note):
     return total, out
 
 
+def cnn_cpu_step_seconds(cfg):
+    """Oracle CNN step on bounded samples: Metropolis with 64 chains x one sweep,
+    E_loc and gradients of 64 samples, a 656^2 x N_s S build (GEMM rate) and a
+    656^2 eigh, extrapolated to the full step."""
+    from oracle import jvmc_oracle as O
+    Lx, Ly = cfg["Lx"], cfg["Ly"]
+    net = O.CNN(F=(3, 3), channels=(8, 8), strides=(1, 1), actFun=("poly4",))
+    rng = np.random.default_rng(0)
+    prm = {k: rng.normal(0, 0.3, sh) for k, sh in net.leaf_shapes((Lx, Ly))}
+    psi = O.NQS(net, prm)
+    H = O.tfim(Lx * Ly, cfg["J"], cfg["h"], lattice=(Lx, Ly))
+    Ns = cfg["chains"] * cfg["per_chain"]
+    n = Lx * Ly
+    chain_steps = cfg["chains"] * (cfg["therm"] + cfg["per_chain"]) * n
+    out = {}
+    C = 64
+    mc = O.MCSampler(psi, (Lx, Ly), 0, numChains=C, numSamples=C, thermalizationSweeps=0, sweepSteps=n)
+    t0 = time.perf_counter()
+    mc.sample(numSamples=C)
+    out["sampling"] = (time.perf_counter() - t0) / (C * n) * chain_steps
+    s = rng.integers(0, 2, (1, 64, Lx, Ly)).astype(np.int32)
+    t0 = time.perf_counter()
+    H.get_O_loc(s, psi)
+    out["eloc"] = (time.perf_counter() - t0) / 64 * Ns
+    t0 = time.perf_counter()
+    g = psi.gradients(s)
+    out["gradients"] = (time.perf_counter() - t0) / 64 * Ns
+    P = g.shape[-1]
+    a = rng.normal(size=(4096, P)) + 0j
+    t0 = time.perf_counter()
+    np.tensordot(np.conj(a), a, axes=(0, 0))
+    out["s_build"] = (time.perf_counter() - t0) * Ns / 4096
+    out["snr"] = out["s_build"]
+    x = rng.normal(size=(P, P))
+    t0 = time.perf_counter()
+    np.linalg.eigh(x @ x.T)
+    out["eigh"] = time.perf_counter() - t0
+    return sum(out.values()), out
+
+
 def cpu_sample_desc(cfg):
+    if cfg.get("net") == "cnn":
+        return ("oracle timed on: CNN Metropolis with 64 chains x one sweep, E_loc and gradients of 64 samples, "
+                "a 656-wide complex GEMM over 4096 samples and the 656^2 eigh; extrapolated to one full step")
     if cfg["sampler"] == "mc":
         return ("oracle (numpy FP64 restatement of jVMC) timed on: Metropolis with 256 chains x two sweeps, "
                 "E_loc and gradients of 512 samples, a 4096^2 x 2048 complex GEMM and a 4096^2 eigh; "
                 "extrapolated to one full step (5.24M chain-steps, 16384 samples, 2P = 33280 GEMMs and eigh)")
     return "oracle timed on 256 exact-basis samples, a 4096^2 x 2048 complex GEMM and a 4096^2 eigh, extrapolated"
+
+
+# ---------------------------------------------------------- replicas (N>1)
+def reduce_max_ms(ms, device=None):
+    """Max over ranks of the timed region (ms); identity without a process group."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(ms)
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t[0])
+
+
+def aggregate_steps_per_s(steps, world, max_ms):
+    """Whole-job throughput of independent replicas: every rank ran ``steps``
+    steps; the job took the slowest rank's time."""
+    return world * steps / (max_ms / 1000.0)
 
 
 # ------------------------------------------------------------------- main
@@ -277,8 +381,9 @@ def kernel_bench(args):
             al, bl = (a - ah.float()).to(torch.bfloat16), (b - bh.float()).to(torch.bfloat16)
             del a, b
             cs = torch.empty(n, dtype=torch.float32, device=dev)
+            ws = torch.empty(L_.query("vmc_gemm_bf16x3_colsq_workspace_bytes", m, n), dtype=torch.uint8, device=dev)
             fn = lambda: L_.call("vmc_gemm_bf16x3_colsq", L_.ptr(ah), L_.ptr(al), m, K, L_.ptr(bh), L_.ptr(bl), n, K,
-                                 K, L_.ptr(cs), st)
+                                 K, L_.ptr(cs), L_.ptr(ws), ws.numel(), st)
             alg = 2.0 * m * n * K
             hw = 3.0 * alg
             shape = {"m": m, "n": n, "k": K}
@@ -316,6 +421,57 @@ def kernel_bench(args):
     emit(out)
 
 
+def quench_bench(args):
+    """XXZ chain H = sum X X + Y Y + 1.5 Z Z (Pauli), L = 48, periodic; CpxRBM
+    M = 96 with bias, started from a Neel-peaked state (hidden unit 0 couples
+    to the staggered magnetisation with weight 1.0 and bias 1.0, the rest
+    N(0, 0.01^2)); N_s = 8192 (1024 chains x 8); real-time TDVP
+    (makeReal='imag', rhsPrefactor=1j) with AdaptiveHeun(tol=1e-4).  Reports
+    the energy drift max_t |E(t) - E(0)| / |E(0)| of each form."""
+    import torch
+    import vmc_jax_gb300 as V
+    torch.cuda.set_device(0)
+    L, M, delta = 48, 96, 1.5
+    rng = np.random.default_rng(0)
+    b = rng.normal(0, 0.01, M) + 1j * rng.normal(0, 0.01, M)
+    W = rng.normal(0, 0.01, (L, M)) + 1j * rng.normal(0, 0.01, (L, M))
+    W[:, 0] = np.array([(-1) ** i for i in range(L)], dtype=float)
+    b[0] = 1.0
+    theta0 = np.concatenate([b.real, b.imag, W.real.ravel(), W.imag.ravel()])
+    H = V.operator.BranchFreeOperator()
+    for l in range(L):
+        r = (l + 1) % L
+        H.add(V.operator.scal_opstr(1.0, (V.operator.Sx(l), V.operator.Sx(r))))
+        H.add(V.operator.scal_opstr(1.0, (V.operator.Sy(l), V.operator.Sy(r))))
+        H.add(V.operator.scal_opstr(delta, (V.operator.Sz(l), V.operator.Sz(r))))
+    res = {}
+    for prec in ["mixed", "fp64"]:
+        psi = V.vqs.NQS(V.nets.CpxRBM(numHidden=M, bias=True), precision="fp64" if prec == "fp64" else "fp32")
+        psi(np.zeros((1, 1, L), np.int32))
+        psi.set_parameters(theta0)
+        smp = V.sampler.MCSampler(psi, (L,), 7, updateProposer=V.sampler.propose_spin_flip, numChains=1024,
+                                  numSamples=8192, thermalizationSweeps=32, sweepSteps=L)
+        td = V.util.TDVP(smp, makeReal="imag", rhsPrefactor=1.j, pinvCutoff=1e-8, snrTol=2, precision=prec)
+        st = V.util.stepper.AdaptiveHeun(timeStep=1e-3, tol=1e-4)
+        theta = psi.get_parameters()
+        t, times, E = 0.0, [], []
+        t0 = time.perf_counter()
+        while t < args.quench:
+            theta, dt = st.step(t, td, theta, hamiltonian=H, psi=psi, numSamples=8192)
+            psi.set_parameters(theta)
+            times.append(t)
+            E.append(float(torch.real(td.ElocMean0)))
+            t += dt
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        E = np.array(E)
+        res[prec] = {"steps": len(E), "t_end": t, "wall_s": wall, "E0": float(E[0]),
+                     "drift": float(np.max(np.abs(E - E[0])) / abs(E[0])), "E": E.tolist(), "t": times}
+    emit({"metric": "XXZ quench energy drift, mixed vs FP64 solve", "workload": "xxz48_rbm96_quench",
+          "config": {"L": L, "M": M, "delta": delta, "num_samples": 8192, "integrator": "AdaptiveHeun tol 1e-4",
+                     "t_end": args.quench}, "data": "synthetic (seeded)", **res})
+
+
 def serve_bench(args):
     """Poisson arrivals of independent jobs (L in {16, 24, 32}, h ~ U[0.5, 1.5],
     M in {1, 2} L, N_s in {2^11, 2^12, 2^13}, ground-state or quench) served by
@@ -351,6 +507,9 @@ def serve_bench(args):
 
 def main():
     args = parse()
+    if args.quench is not None:
+        quench_bench(args)
+        return
     if args.serve:
         serve_bench(args)
         return
@@ -400,12 +559,7 @@ def main():
     clock = clocks.stop()
     TIMER.enabled = False
     launches = V._lib.launch_count
-    ms = t_start.elapsed_time(t_end)
-    if world > 1:
-        import torch.distributed as dist
-        tt = torch.tensor([ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms = float(tt[0])
+    ms = reduce_max_ms(t_start.elapsed_time(t_end), device=torch.device("cuda", local))
     ms_per_step = ms / args.steps
     phases = {k: v / args.steps for k, v in TIMER.durations().items()}
     gram_ms = TIMER.spans("gram_kernel")
@@ -437,7 +591,7 @@ def main():
             peaks = json.load(f)
     except Exception:
         pass
-    L, M, Ns, P = cfg["L"], cfg["M"], ctx["ns"], ctx["P"]
+    Ns, P = ctx["ns"], ctx["P"]
     roofline = None
     if gram_ms:
         t = float(np.mean(gram_ms)) * 1e-3
@@ -456,7 +610,8 @@ def main():
                     "traffic": traffic, "algorithmic_flops_per_launch": flops,
                     "hardware_flops_per_launch": 3 * 2.0 * Ns * (2 * P) ** 2 / 2,
                     "launch_ms": t * 1e3}
-    out = {"metric": "TDVP steps/s", "value": 1000.0 / ms_per_step, "unit": "steps/s", "n_gpus": world,
+    out = {"metric": "TDVP steps/s", "value": aggregate_steps_per_s(args.steps, world, ms), "unit": "steps/s",
+           "n_gpus": world,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32+bf16x3 (FP64 statistics and eigensolve)",
            "data": "synthetic (seeded lattice and parameters)",

@@ -318,9 +318,14 @@ int vmc_gram_bf16x3(const void* hi, const void* lo, int32_t rows, int32_t k, int
 
 /* SNR transform (stats.py:75-83 via tdvp.py:175-179): colsq[c] =
  * sum_r (sum_j A[r][j] B[c][j])^2 for A (m x k) and B (n x k) given as hi/lo
- * planes; colsq (n floats) is overwritten; the product is never stored. */
+ * planes; colsq (n floats) is overwritten; the product is never stored.
+ * Partial sums per 128-row tile and warp go to the workspace
+ * (vmc_gemm_bf16x3_colsq_workspace_bytes) and are added in a fixed order:
+ * the result is bitwise reproducible. */
+size_t vmc_gemm_bf16x3_colsq_workspace_bytes(int32_t m, int32_t n);
 int vmc_gemm_bf16x3_colsq(const void* a_hi, const void* a_lo, int32_t m, int64_t lda, const void* b_hi,
-                          const void* b_lo, int32_t n, int64_t ldb, int32_t k, float* colsq, vmc_stream_t stream);
+                          const void* b_lo, int32_t n, int64_t ldb, int32_t k, float* colsq, void* workspace,
+                          size_t workspace_bytes, vmc_stream_t stream);
 
 /* Error flag of the tensor-core kernels (a bounded wait that ran out);
  * synchronises the device.  reset != 0 clears it. */

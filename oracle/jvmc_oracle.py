@@ -1050,7 +1050,7 @@ def measure(observables, psi, sampler, numSamples=None):
 
 def ground_state_search(psi, ham, tdvpEquation, sampler, numSteps=200, varianceTol=1e-10, stepSize=1e-2):
     """util.py:160-212 without output management."""
-    delta = tdvpEquation.diagonalShift
+    delta = getattr(tdvpEquation, "diagonalShift", 0.)
     stepper = Euler(timeStep=stepSize)
     n = 0
     varE = 1.0
@@ -1059,6 +1059,64 @@ def ground_state_search(psi, ham, tdvpEquation, sampler, numSteps=200, varianceT
         psi.set_parameters(dp)
         n += 1
         varE = tdvpEquation.get_energy_variance()
-        delta = 0.95 * delta
-        tdvpEquation.set_diagonal_shift(delta)
+        if hasattr(tdvpEquation, "set_diagonal_shift"):
+            delta = 0.95 * delta
+            tdvpEquation.set_diagonal_shift(delta)
     return n
+
+
+# ---------------------------------------------------------------------------
+# MinSR (jVMC/util/minsr.py)
+# ---------------------------------------------------------------------------
+
+def pinv_hermitian(T, rtol):
+    """Pseudo-inverse of a Hermitian matrix through its eigendecomposition,
+    dropping |eigenvalues| <= rtol * max |eigenvalue| (jnp.linalg.pinv with
+    hermitian=True, as called at minsr.py:63,74)."""
+    ev, V = np.linalg.eigh(T)
+    cut = rtol * np.max(np.abs(ev))
+    inv = np.where(np.abs(ev) > cut, 1.0 / ev, 0.0)
+    return (V * inv) @ np.conj(V.T)
+
+
+class MinSR:
+    """minsr.py:16-165 for one device."""
+
+    def __init__(self, sampler, pinvTol=1e-14, diagonalShift=0.):
+        self.sampler = sampler
+        self.pinvTol = pinvTol
+        self.diagonalShift = diagonalShift
+
+    def solve(self, eloc, gradients, holomorphic):  # minsr.py:53-80
+        if holomorphic:
+            T = gradients.tangent_kernel()
+            T_inv = pinv_hermitian(T, self.pinvTol)
+            e = eloc._data.reshape((-1,))
+            G = gradients._data.reshape((-1,) + gradients._data.shape[2:])
+            return -np.conj(G).T @ T_inv @ e
+        G = gradients._data.reshape((-1,) + gradients._data.shape[2:])
+        G = np.concatenate([np.real(G), np.imag(G)], axis=0)
+        T = G @ G.T + self.diagonalShift * np.eye(G.shape[0])
+        T_inv = pinv_hermitian(T, self.pinvTol)
+        e = eloc._data.reshape((-1,))
+        e = np.concatenate([np.real(e), np.imag(e)], axis=0)
+        return -G.T @ T_inv @ e
+
+    def __call__(self, netParameters, t, *, psi, hamiltonian, **rhsArgs):  # minsr.py:82-165
+        tmp = psi.get_parameters()
+        psi.set_parameters(netParameters)
+        configs, logPsi, p = self.sampler.sample(numSamples=rhsArgs.get("numSamples", None))
+        Eloc = SampledObs(hamiltonian.get_O_loc(configs, psi, logPsi, t), p)
+        grads = SampledObs(psi.gradients(configs), p)
+        update = self.solve(Eloc, grads, holomorphic=psi.holomorphic)
+        psi.set_parameters(tmp)
+        if rhsArgs.get("intStep", None) == 0:
+            self.ElocMean0 = Eloc.mean()[0]
+            self.ElocVar0 = Eloc.var()[0]
+        return update
+
+    def get_energy_variance(self):
+        return self.ElocVar0
+
+    def get_energy_mean(self):
+        return np.real(self.ElocMean0)

@@ -154,3 +154,29 @@ def test_cross_validation_runs(cuda):
     md = td.get_metadata()
     assert np.isfinite(float(md["tdvp_residual_cross_validation_ratio"]))
     assert np.isfinite(float(md["tdvp_error_cross_validation_ratio"]))
+
+
+@pytest.mark.parametrize("k", [0, 1])
+def test_minsr_gs_search(cuda, fixtures, k):
+    """tests/minsr_test.py:15-43 through the CUDA path (exEs within 1e-3)."""
+    import vmc_jax_gb300 as V
+    hx, exE = fixtures["tdvp_gs_hxs"][k], fixtures["tdvp_exEs"][k]
+    psi = V.vqs.NQS(V.nets.CpxRBM(numHidden=8, bias=False), seed=1234)
+    H = _tfim(V, 4, 1.0, -hx)
+    es = V.sampler.ExactSampler(psi, 4)
+    solver = V.util.MinSR(es, pinvTol=1e-6, diagonalShift=0.)
+    V.util.ground_state_search(psi, H, solver, es, numSteps=200, stepSize=1e-2)
+    E = float(V.util.measure({'energy': H}, psi, es)['energy']['mean'][0])
+    assert abs((E - exE) / exE) < 1e-3
+
+
+def test_minsr_update_matches_oracle(cuda):
+    import vmc_jax_gb300 as V
+    psi, opsi = _pair(8, 6, True, 0.2, seed=9)
+    H = _tfim(V, 8, 1.0, 0.9)
+    es = V.sampler.ExactSampler(psi, 8)
+    eso = O.ExactSampler(opsi, 8)
+    u = V.util.MinSR(es, pinvTol=1e-8)(psi.get_parameters(), 0., psi=psi, hamiltonian=H, intStep=0)
+    uo = O.MinSR(eso, pinvTol=1e-8)(opsi.get_parameters(), 0., psi=opsi, hamiltonian=O.tfim(8, 1.0, 0.9),
+                                    intStep=0)
+    assert _rel(u.cpu().numpy(), uo) < 1e-8

@@ -60,9 +60,14 @@ def test_gemm_bf16x3_colsq(cuda, m, n, k):
     ah, al = _planes(a, ld)
     bh, bl = _planes(b, ld)
     colsq = torch.full((n,), float("nan"), dtype=torch.float32, device=cuda)
+    ws = torch.empty(L.query("vmc_gemm_bf16x3_colsq_workspace_bytes", m, n), dtype=torch.uint8, device=cuda)
     L.call("vmc_gemm_bf16x3_colsq", L.ptr(ah), L.ptr(al), m, ld, L.ptr(bh), L.ptr(bl), n, ld, k, L.ptr(colsq),
-           L.stream())
+           L.ptr(ws), ws.numel(), L.stream())
+    first = colsq.clone()
+    L.call("vmc_gemm_bf16x3_colsq", L.ptr(ah), L.ptr(al), m, ld, L.ptr(bh), L.ptr(bl), n, ld, k, L.ptr(colsq),
+           L.ptr(ws), ws.numel(), L.stream())
     torch.cuda.synchronize()
+    assert torch.equal(first, colsq)  # fixed-order reduction: bitwise reproducible
     assert L.query("vmc_tc_error_flag", 1) == 0
     D = _split_product(ah, al, bh, bl, k)
     ref = (D ** 2).sum(0)

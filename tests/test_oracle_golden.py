@@ -181,3 +181,17 @@ def test_exact_sampler_energy_matches_ed():
         v = np.exp(lp[0])
         Hm = O.hamiltonian_matrix(H, L)
         assert abs(E - np.vdot(v, Hm @ v) / np.vdot(v, v)) < 1e-10
+
+
+@pytest.mark.parametrize("k", [0, 1])
+def test_minsr_gs_search(fixtures, k):
+    """tests/minsr_test.py:15-43: MinSR ground-state search to exEs (1e-3)."""
+    hx, exE = fixtures["tdvp_gs_hxs"][k], fixtures["tdvp_exEs"][k]
+    rng = np.random.default_rng(1234)
+    psi = O.NQS(O.CpxRBM(8, False), O.init_cpx_rbm(4, 8, False, rng, dist="uniform"))
+    H = O.tfim(4, 1.0, -hx)
+    es = O.ExactSampler(psi, 4)
+    solver = O.MinSR(es, pinvTol=1e-6, diagonalShift=0.)
+    O.ground_state_search(psi, H, solver, es, numSteps=200, stepSize=1e-2)
+    E = O.measure({'energy': H}, psi, es)['energy']['mean'][0]
+    assert abs((E - exE) / exE) < 1e-3

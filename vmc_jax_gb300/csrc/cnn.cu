@@ -264,7 +264,7 @@ __global__ void cnn_metropolis_kernel(int32_t* __restrict__ states, int C, cnn_g
     double nw = (double)warp_output(g, z, lane);
     nw = __shfl_sync(0xffffffffu, nw, 0);
     const double P = exp(mu * nw - mu * cur);
-    if (d.u < P) {
+    if (d.u64() < P) {
       if (lane == 0) cfg[d.site] = (int8_t)(1 - cfg[d.site]);
       cur = nw;
       ++accepted;

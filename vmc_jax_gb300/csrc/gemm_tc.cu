@@ -135,7 +135,7 @@ struct tc_args {
   int M, N, K;        // D is M x N, reduction over K (operand rows are K-contiguous)
   int mode;           // 0: store upper tiles of a symmetric product, 1: column sums of squares
   int tilesM, tilesN;
-  float* out;         // mode 0: D (row-major, ld = ldOut); mode 1: colsq (N)
+  float* out;         // mode 0: D (row-major, ld = ldOut); mode 1: partial column sums (tilesM * 4, N)
   int64_t ldOut;
 };
 
@@ -275,11 +275,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             }
           }
         } else {
+          // per-(row tile, warp) partial column sums, reduced later in a
+          // fixed order (bitwise reproducible, no atomics)
+          float* part = a.out + ((int64_t)tm * 4 + q) * a.N;
 #pragma unroll
           for (int i = 0; i < 16; ++i) {
             float s2 = gr < a.M ? v[i] * v[i] : 0.f;
             s2 = warp_sum(s2);
-            if (lane == 0 && gc + i < a.N) atomicAdd(a.out + gc + i, s2);
+            if (lane == 0 && gc + i < a.N) part[gc + i] = s2;
           }
         }
       }
@@ -372,19 +375,34 @@ extern "C" int vmc_gram_bf16x3(const void* hi, const void* lo, int32_t rows, int
   return launch_tc(mh, ml, nh, nl, a, (int)grid, as_stream(stream));
 }
 
+namespace vmc {
+// colsq[c] = sum over (row tile, warp) partials in a fixed order, FP64 accumulation
+__global__ void colsq_reduce_kernel(const float* __restrict__ part, int nparts, int n, float* __restrict__ colsq) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int r = 0; r < nparts; ++r) s += (double)part[(int64_t)r * n + c];
+    colsq[c] = (float)s;
+  }
+}
+}  // namespace vmc
+
+extern "C" size_t vmc_gemm_bf16x3_colsq_workspace_bytes(int32_t m, int32_t n) {
+  return (size_t)((m + TC_BM - 1) / TC_BM) * 4 * (size_t)n * sizeof(float) + 256;
+}
+
 extern "C" int vmc_gemm_bf16x3_colsq(const void* a_hi, const void* a_lo, int32_t m, int64_t lda, const void* b_hi,
                                      const void* b_lo, int32_t n, int64_t ldb, int32_t k, float* colsq,
-                                     vmc_stream_t stream) {
+                                     void* workspace, size_t workspace_bytes, vmc_stream_t stream) {
   VMC_REQUIRE(a_hi && a_lo && b_hi && b_lo && colsq && m > 0 && n > 0 && k > 0, VMC_ERR_INVALID_ARGUMENT,
               "vmc_gemm_bf16x3_colsq: bad arguments");
+  VMC_REQUIRE(workspace && workspace_bytes >= vmc_gemm_bf16x3_colsq_workspace_bytes(m, n), VMC_ERR_WORKSPACE,
+              "vmc_gemm_bf16x3_colsq: workspace of %zu bytes needed", vmc_gemm_bf16x3_colsq_workspace_bytes(m, n));
   CUtensorMap ah, al, bh, bl;
   int rc;
   if ((rc = make_map(&ah, a_hi, m, k, lda, TC_BM))) return rc;
   if ((rc = make_map(&al, a_lo, m, k, lda, TC_BM))) return rc;
   if ((rc = make_map(&bh, b_hi, n, k, ldb, TC_BN))) return rc;
   if ((rc = make_map(&bl, b_lo, n, k, ldb, TC_BN))) return rc;
-  cudaError_t e = cudaMemsetAsync(colsq, 0, sizeof(float) * (size_t)n, as_stream(stream));
-  VMC_REQUIRE(e == cudaSuccess, VMC_ERR_CUDA, "vmc_gemm_bf16x3_colsq: %s", cudaGetErrorString(e));
   tc_args a;
   a.M = m;
   a.N = n;
@@ -392,9 +410,13 @@ extern "C" int vmc_gemm_bf16x3_colsq(const void* a_hi, const void* a_lo, int32_t
   a.mode = 1;
   a.tilesM = (m + TC_BM - 1) / TC_BM;
   a.tilesN = (n + TC_BN - 1) / TC_BN;
-  a.out = colsq;
+  a.out = reinterpret_cast<float*>(workspace);
   a.ldOut = 0;
-  return launch_tc(ah, al, bh, bl, a, a.tilesM * a.tilesN, as_stream(stream));
+  int rc2 = launch_tc(ah, al, bh, bl, a, a.tilesM * a.tilesN, as_stream(stream));
+  if (rc2) return rc2;
+  colsq_reduce_kernel<<<(n + 255) / 256, 256, 0, as_stream(stream)>>>(reinterpret_cast<const float*>(workspace),
+                                                                       a.tilesM * 4, n, colsq);
+  return check_launch("vmc_gemm_bf16x3_colsq(reduce)");
 }
 
 extern "C" int vmc_tc_error_flag(int32_t reset) {

@@ -170,6 +170,7 @@ __global__ void rbm_oloc_fused_kernel(const int32_t* __restrict__ configs, int64
   cpx<T>* th = reinterpret_cast<cpx<T>*>(base + warp * perWarpAligned);
   uint32_t* occ = reinterpret_cast<uint32_t*>(th + p.M);
   int8_t* cfg = reinterpret_cast<int8_t*>(occ + nw);
+  int16_t* fsites = reinterpret_cast<int16_t*>(base + kWarpsPerBlock * perWarpAligned);
 
   for (int w = threadIdx.x; w < diagWords; w += blockDim.x) isdiag[w] = 0u;
   __syncthreads();
@@ -205,71 +206,90 @@ __global__ void rbm_oloc_fused_kernel(const int32_t* __restrict__ configs, int64
     }
     __syncwarp();
 
+    // Strings are handled 32 at a time, lane k applying string c0 + k (the
+    // matrix elements are complex128: one FP64 instruction covers 32
+    // strings); then, for each nonzero off-diagonal string of the chunk, the
+    // whole warp forms psi(s')/psi(s) over the hidden units.
     cpx<double> diagSum = mk(0.0, 0.0);
     cpx<double> acc = mk(0.0, 0.0);
-    bf_string_result r;
-    for (int o = 0; o < op.num_ops; ++o) {
-      bf_apply_string(op, o, cfg, occ, p.L, r);
-      if ((isdiag[o >> 5] >> (o & 31)) & 1u) {
-        diagSum = diagSum + r.m;
-        continue;
-      }
-      if (!(sqrt(abs2(r.m)) > 1e-6)) continue;  // _find_nonzero threshold (base.py:96)
-      int fs[VMC_BF_MAX_LEN];
+    int16_t* fsRow = fsites + (size_t)warp * 32 * VMC_BF_MAX_LEN;
+    for (int c0 = 0; c0 < op.num_ops; c0 += 32) {
+      const int o = c0 + lane;
+      bool valid = false;
       int nf = 0;
-      for (int q = 0; q < r.nmod; ++q)
-        if (r.val[q] != cfg[r.site[q]]) fs[nf++] = r.site[q];
-      if (nf == 0) {
-        acc = acc + r.m;
-        continue;
-      }
-      scaled_cpx<T> prod;
-      prod.m = mk(T(1), T(0));
-      prod.ex = 0;
-      int cnt = 0;
-      if (nf == 1) {
-        const int i = fs[0];
-        const T sg = cfg[i] ? T(1) : T(-1);
-        const cpx<T>* rc = tC + (size_t)i * p.M;
-        const cpx<T>* rs = tS + (size_t)i * p.M;
-        for (int j = lane; j < p.M; j += 32) {
-          cpx<T> t = th[j];
-          cpx<T> f = rc[j] - sg * (t * rs[j]);
-          prod.m = prod.m * f;
-          if (++cnt == 8) {
-            renorm(prod);
-            cnt = 0;
-          }
+      cpx<double> m = mk(0.0, 0.0);
+      if (o < op.num_ops) {
+        bf_string_result r;
+        bf_apply_string(op, o, cfg, occ, p.L, r);
+        if ((isdiag[o >> 5] >> (o & 31)) & 1u) {
+          diagSum = diagSum + r.m;
+        } else if (sqrt(abs2(r.m)) > 1e-6) {  // _find_nonzero threshold (base.py:96)
+          valid = true;
+          m = r.m;
+          for (int q = 0; q < r.nmod; ++q)
+            if (r.val[q] != cfg[r.site[q]]) fsRow[lane * VMC_BF_MAX_LEN + nf++] = (int16_t)r.site[q];
         }
-      } else {
-        for (int j = lane; j < p.M; j += 32) {
-          cpx<T> e1 = mk(T(1), T(0)), e2 = mk(T(1), T(0));
-          for (int q = 0; q < nf; ++q) {
-            const int i = fs[q];
-            cpx<T> a = tEp[(size_t)i * p.M + j], b = tEm[(size_t)i * p.M + j];
-            if (cfg[i]) {
-              e1 = e1 * b;
-              e2 = e2 * a;
-            } else {
-              e1 = e1 * a;
-              e2 = e2 * b;
+      }
+      __syncwarp();
+      unsigned vmask = __ballot_sync(0xffffffffu, valid);
+      const int myNf = nf;
+      cpx<T> myRatio = mk(T(1), T(0));
+      while (vmask) {
+        const int k = __ffs(vmask) - 1;
+        vmask &= vmask - 1;
+        const int nfk = __shfl_sync(0xffffffffu, myNf, k);
+        if (nfk == 0) continue;  // flips cancel: psi(s') / psi(s) = 1
+        const int16_t* fs = fsRow + k * VMC_BF_MAX_LEN;
+        scaled_cpx<T> prod;
+        prod.m = mk(T(1), T(0));
+        prod.ex = 0;
+        int cnt = 0;
+        if (nfk == 1) {
+          const int i = fs[0];
+          const T sg = cfg[i] ? T(1) : T(-1);
+          const cpx<T>* rc = tC + (size_t)i * p.M;
+          const cpx<T>* rs = tS + (size_t)i * p.M;
+          for (int j = lane; j < p.M; j += 32) {
+            cpx<T> f = rc[j] - sg * (th[j] * rs[j]);
+            prod.m = prod.m * f;
+            if (++cnt == 8) {
+              renorm(prod);
+              cnt = 0;
             }
           }
-          cpx<T> t = th[j];
-          cpx<T> onep = mk(T(1) + t.re, t.im), onem = mk(T(1) - t.re, -t.im);
-          cpx<T> f = T(0.5) * (onep * e1 + onem * e2);
-          prod.m = prod.m * f;
-          if (++cnt == 8) {
-            renorm(prod);
-            cnt = 0;
+        } else {
+          for (int j = lane; j < p.M; j += 32) {
+            cpx<T> e1 = mk(T(1), T(0)), e2 = mk(T(1), T(0));
+            for (int q = 0; q < nfk; ++q) {
+              const int i = fs[q];
+              cpx<T> a = tEp[(size_t)i * p.M + j], b = tEm[(size_t)i * p.M + j];
+              if (cfg[i]) {
+                e1 = e1 * b;
+                e2 = e2 * a;
+              } else {
+                e1 = e1 * a;
+                e2 = e2 * b;
+              }
+            }
+            cpx<T> t = th[j];
+            cpx<T> onep = mk(T(1) + t.re, t.im), onem = mk(T(1) - t.re, -t.im);
+            cpx<T> f = T(0.5) * (onep * e1 + onem * e2);
+            prod.m = prod.m * f;
+            if (++cnt == 8) {
+              renorm(prod);
+              cnt = 0;
+            }
           }
         }
+        renorm(prod);
+        prod = warp_prod(prod);
+        if (lane == k) myRatio = to_cpx(prod);
       }
-      renorm(prod);
-      prod = warp_prod(prod);
-      cpx<T> ratio = to_cpx(prod);
-      acc = acc + r.m * mk((double)ratio.re, (double)ratio.im);
+      if (valid) acc = acc + m * mk((double)myRatio.re, (double)myRatio.im);
+      __syncwarp();
     }
+    acc = warp_sum(acc);
+    diagSum = warp_sum(diagSum);
     if (op.num_diag > 0 && sqrt(abs2(diagSum)) > 1e-6) acc = acc + diagSum;
     if (logPsiS) {
       // O_loc = sum_k m_k psi(s'_k)/psi_net(s) * exp(log psi_net(s) - log psi_given(s))
@@ -537,7 +557,7 @@ extern "C" int vmc_rbm_oloc_fused(int32_t precision, const int32_t* configs, int
   size_t perWarp = (size_t)num_hidden * el + (size_t)nw * 4 + ((num_sites + 15) & ~15);
   perWarp = (perWarp + 15) & ~(size_t)15;
   const size_t diagBytes = ((((op->num_ops + 31) >> 5) * 4) + 15) & ~15;
-  size_t smem = diagBytes + kWarpsPerBlock * perWarp;
+  size_t smem = diagBytes + kWarpsPerBlock * perWarp + (size_t)kWarpsPerBlock * 32 * VMC_BF_MAX_LEN * 2;
   VMC_REQUIRE(smem <= 227 * 1024, VMC_ERR_UNSUPPORTED, "vmc_rbm_oloc_fused: M=%d, %d strings too large", num_hidden,
               op->num_ops);
   int grid = grid_for(num_configs);
@@ -668,9 +688,26 @@ __global__ void __launch_bounds__(256) rbm_metropolis_kernel(
   const T halfMu = T(0.5 * mu);
   unsigned long long accepted = 0;
   const int64_t total = thermSteps + sweepSteps * samplesPerChain;
+  // the flip site does not depend on the chain state: the next step's table
+  // rows are loaded while the current step is evaluated
+  mc_draw d = metropolis_draw(seed, call, 0u, (uint32_t)chain, L);
+  cpx<T> fC[JPL], fS[JPL];
+#pragma unroll
+  for (int q = 0; q < JPL; ++q) {
+    const int j = lane + 32 * q;
+    fC[q] = j < M ? tC[(size_t)d.site * M + j] : mk(T(1), T(0));
+    fS[q] = j < M ? tS[(size_t)d.site * M + j] : mk(T(0), T(0));
+  }
   for (int64_t step = 0; step < total; ++step) {
-    const mc_draw d = metropolis_draw(seed, call, (uint32_t)step, (uint32_t)chain, L);
     const int i = d.site;
+    const mc_draw dn = metropolis_draw(seed, call, (uint32_t)(step + 1), (uint32_t)chain, L);
+    cpx<T> nC[JPL], nS[JPL];
+#pragma unroll
+    for (int q = 0; q < JPL; ++q) {
+      const int j = lane + 32 * q;
+      nC[q] = j < M ? tC[(size_t)dn.site * M + j] : mk(T(1), T(0));
+      nS[q] = j < M ? tS[(size_t)dn.site * M + j] : mk(T(0), T(0));
+    }
     const T sg = cfg[i] ? T(1) : T(-1);
     // |ratio|^2 over this lane's hidden units, as mantissa * 2^ex
     T prod = T(1);
@@ -679,7 +716,7 @@ __global__ void __launch_bounds__(256) rbm_metropolis_kernel(
     for (int q = 0; q < JPL; ++q) {
       const int j = lane + 32 * q;
       if (j < M) {
-        cpx<T> f = tC[(size_t)i * M + j] - sg * (tn[q] * tS[(size_t)i * M + j]);
+        cpx<T> f = fC[q] - sg * (tn[q] * fS[q]);
         prod *= abs2(f);
         if ((q & 3) == 3) {
           int e = exponent_of(prod);
@@ -712,10 +749,17 @@ __global__ void __launch_bounds__(256) rbm_metropolis_kernel(
     // one decision for the whole warp: lane 0's value
     prod = __shfl_sync(0xffffffffu, prod, 0);
     ex = __shfl_sync(0xffffffffu, ex, 0);
-    // P = |ratio|^mu = (prod * 2^ex)^(mu/2)
-    const double logr2 = log((double)prod) + (double)ex * 0.69314718055994530942;
-    const double P = exp((double)halfMu * logr2);
-    const bool acc = d.u < P;
+    bool acc;
+    if (sizeof(T) == sizeof(double)) {
+      // P = |ratio|^mu = (prod * 2^ex)^(mu/2); accept iff u < P (bernoulli, sampler.py:339-340)
+      const double logr2 = log((double)prod) + (double)ex * 0.69314718055994530942;
+      const double P = exp((double)halfMu * logr2);
+      acc = d.u64() < P;
+    } else {
+      const float lg2 = log2f((float)prod) + (float)ex;
+      const float P = exp2f((float)halfMu * lg2);
+      acc = d.u32() < P;
+    }
     if (acc) {
 #pragma unroll
       for (int q = 0; q < JPL; ++q) {
@@ -731,6 +775,12 @@ __global__ void __launch_bounds__(256) rbm_metropolis_kernel(
       __syncwarp();
       ++accepted;
     }
+#pragma unroll
+    for (int q = 0; q < JPL; ++q) {
+      fC[q] = nC[q];
+      fS[q] = nS[q];
+    }
+    d = dn;
     if (step >= thermSteps && ((step - thermSteps + 1) % sweepSteps) == 0) {
       const int64_t s = (step - thermSteps + 1) / sweepSteps - 1;
       int32_t* out = configsOut + ((size_t)s * C + chain) * L;

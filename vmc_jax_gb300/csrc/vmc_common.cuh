@@ -219,10 +219,16 @@ __host__ __device__ __forceinline__ u32x4 philox4x32_10(u32x4 c, uint32_t k0, ui
   return c;
 }
 
-// One Metropolis draw: flip site in [0, L) and a uniform double in [0, 1).
+// One Metropolis draw: flip site in [0, L) and the acceptance uniform,
+// as a 53-bit double ((r1>>5) 2^26 + (r2>>6)) / 2^53 (FP64 kernels) or a
+// 24-bit float (r1>>8) / 2^24 (FP32 kernels).
 struct mc_draw {
   int site;
-  double u;
+  uint32_t r1, r2;
+  __device__ __forceinline__ double u64() const {
+    return ((double)(r1 >> 5) * 67108864.0 + (double)(r2 >> 6)) * (1.0 / 9007199254740992.0);
+  }
+  __device__ __forceinline__ float u32() const { return (float)(r1 >> 8) * (1.0f / 16777216.0f); }
 };
 
 __device__ __forceinline__ mc_draw metropolis_draw(uint64_t seed, uint32_t call, uint32_t step, uint32_t chain,
@@ -235,7 +241,8 @@ __device__ __forceinline__ mc_draw metropolis_draw(uint64_t seed, uint32_t call,
   u32x4 r = philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
   mc_draw d;
   d.site = (int)(((uint64_t)r.x * (uint64_t)L) >> 32);
-  d.u = ((double)(r.y >> 5) * 67108864.0 + (double)(r.z >> 6)) * (1.0 / 9007199254740992.0);
+  d.r1 = r.y;
+  d.r2 = r.z;
   return d;
 }
 

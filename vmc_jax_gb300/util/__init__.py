@@ -1,7 +1,8 @@
 """Solvers, integrators and drivers (mirror of jVMC.util)."""
 
 from .tdvp import TDVP, realFun, imagFun
+from .minsr import MinSR
 from . import stepper
 from .util import measure, ground_state_search
 
-__all__ = ["TDVP", "realFun", "imagFun", "stepper", "measure", "ground_state_search"]
+__all__ = ["TDVP", "MinSR", "realFun", "imagFun", "stepper", "measure", "ground_state_search"]

@@ -49,8 +49,9 @@ def mixed_snr_colsq(flat, w, okMean, E, emean, f, U, prec, N, L, M, P, Wk, bk, x
     bl = torch.empty((R, ld), dtype=torch.bfloat16, device=dev)
     _lib.call("vmc_eigvec_bf16x2", _lib.ptr(U), U.stride(1), P, _lib.ptr(bh), _lib.ptr(bl), ld, st)
     colsq = torch.empty(R, dtype=torch.float32, device=dev)
+    ws = _lib.Workspace.get(_lib.query("vmc_gemm_bf16x3_colsq_workspace_bytes", N, R))
     TIMER.mark("snr_kernel")
     _lib.call("vmc_gemm_bf16x3_colsq", _lib.ptr(hh), _lib.ptr(hl), N, ld, _lib.ptr(bh), _lib.ptr(bl), R, ld, R,
-              _lib.ptr(colsq), st)
+              _lib.ptr(colsq), _lib.ptr(ws), ws.numel(), st)
     TIMER.mark("snr_kernel_end")
     return colsq

@@ -160,12 +160,16 @@ class NQS:
         """vqs.py:430-444."""
         if not isinstance(P, torch.Tensor):
             P = torch.as_tensor(np.asarray(P))
-        P = P.to(device=global_defs.device(), dtype=torch.float64)
+        cplx = P.is_complex()
+        P = P.to(device=global_defs.device(), dtype=torch.complex128 if cplx else torch.float64)
         out = {}
         start = 0
         for (name, p), (n, shape) in zip(self.params.items(), self.paramShapes):
             if not self.realParams:
-                out[name] = torch.complex(P[start:start + n], P[start + n:start + 2 * n]).reshape(shape)
+                if cplx:  # P[a] + 1j * P[b] in complex arithmetic, as vqs.py:437
+                    out[name] = (P[start:start + n] + 1.j * P[start + n:start + 2 * n]).reshape(shape)
+                else:
+                    out[name] = torch.complex(P[start:start + n], P[start + n:start + 2 * n]).reshape(shape)
                 start += 2 * n
             else:
                 out[name] = P[start:start + n].reshape(shape).clone()
