@@ -39,6 +39,8 @@ WORKLOADS = {
     "ising10_rbm20_exact": dict(L=10, M=20, J=1.0, h=0.7, dt=0.01, sampler="exact"),
     "ising10x10_cnn8x8_mcmc32k": dict(Lx=10, Ly=10, J=1.0, h=3.0, chains=4096, therm=10, per_chain=8, dt=0.01,
                                        sampler="mc", net="cnn"),
+    "ising64_symrbm64_mcmc16k": dict(L=64, M=64, J=1.0, h=1.0, chains=1024, therm=64, per_chain=16, dt=0.01,
+                                     sampler="mc", net="symrbm", symmetries=("translation",)),
 }
 DEFAULT_WORKLOAD = "ising64_rbm256_mcmc16k"
 
@@ -61,7 +63,10 @@ def parse():
     ap.add_argument("--quench", type=float, default=None,
                     help="XXZ L=48 real-time quench with the adaptive Heun integrator up to this time: energy drift "
                          "of the mixed form and of the FP64 form")
-    ap.add_argument("--kernel", default=None, choices=["gram", "snr", "eloc", "metropolis"],
+    ap.add_argument("--quench-steps", type=int, default=40, help="step cap of each quench integration")
+    ap.add_argument("--quench-wall", type=float, default=240.0, help="wall-clock cap (s) of each quench integration")
+    ap.add_argument("--kernel", default=None,
+                    choices=["gram", "snr", "eloc", "metropolis", "data", "hermitian", "gemv", "stats"],
                     help="time one kernel on a fixed synthetic case instead of the TDVP step (profiling)")
     return ap.parse_args()
 
@@ -119,7 +124,11 @@ def build(cfg, precision):
     if cfg.get("net") == "cnn":
         return build_cnn(cfg, precision)
     L, M = cfg["L"], cfg["M"]
-    psi = V.vqs.NQS(V.nets.CpxRBM(numHidden=M, bias=True), precision="fp64" if precision == "fp64" else "fp32")
+    orbit = None
+    if cfg.get("net") == "symrbm":
+        orbit = V.util.symmetries.get_orbit_1D(L, *cfg["symmetries"])
+    psi = V.vqs.NQS(V.nets.CpxRBM(numHidden=M, bias=True), orbit=orbit,
+                    precision="fp64" if precision == "fp64" else "fp32")
     psi(np.zeros((1, 1, L), np.int32))
     psi.set_parameters(initial_parameters(cfg))
     H = V.operator.BranchFreeOperator()
@@ -207,22 +216,27 @@ def cpu_step_seconds(cfg, budget_note):
     L, M = cfg["L"], cfg["M"]
     rng = np.random.default_rng(0)
     prm = O.init_cpx_rbm(L, M, True, rng, scale=0.01)
-    psi = O.NQS(O.CpxRBM(M, True), prm)
+    sym = cfg.get("net") == "symrbm"
+    if sym:
+        orbit, factor = O.get_orbit_1D(L, *cfg["symmetries"])
+        psi = O.NQS(O.SymNet(O.CpxRBM(M, True), orbit, factor), prm)
+    else:
+        psi = O.NQS(O.CpxRBM(M, True), prm)
     H = O.tfim(L, cfg["J"], cfg["h"])
     P2 = 2 * (L * M + M)
     out = {}
     if cfg["sampler"] == "mc":
         Ns = cfg["chains"] * cfg["per_chain"]
         chain_steps = cfg["chains"] * (cfg["therm"] + cfg["per_chain"]) * L
-        C = 256
-        mc = O.MCSampler(psi, (L,), 0, numChains=C, numSamples=2 * C, thermalizationSweeps=0, sweepSteps=L)
+        C, sweeps = (64, 1) if sym else (256, 2)
+        mc = O.MCSampler(psi, (L,), 0, numChains=C, numSamples=sweeps * C, thermalizationSweeps=0, sweepSteps=L)
         t0 = time.perf_counter()
-        mc.sample(numSamples=2 * C)
-        out["sampling"] = (time.perf_counter() - t0) / (2 * C * L) * chain_steps
+        mc.sample(numSamples=sweeps * C)
+        out["sampling"] = (time.perf_counter() - t0) / (sweeps * C * L) * chain_steps
     else:
         Ns = 2 ** L
         out["sampling"] = 0.0
-    n_s = 512 if cfg["sampler"] == "mc" else min(Ns, 256)
+    n_s = (64 if sym else 512) if cfg["sampler"] == "mc" else min(Ns, 256)
     s = rng.integers(0, 2, (1, n_s, L)).astype(np.int32)
     t0 = time.perf_counter()
     H.get_O_loc(s, psi)
@@ -291,6 +305,10 @@ def cpu_sample_desc(cfg):
     if cfg.get("net") == "cnn":
         return ("oracle timed on: CNN Metropolis with 64 chains x one sweep, E_loc and gradients of 64 samples, "
                 "a 656-wide complex GEMM over 4096 samples and the 656^2 eigh; extrapolated to one full step")
+    if cfg.get("net") == "symrbm":
+        return ("oracle (numpy FP64 restatement of jVMC, SymNet over %d translations) timed on: Metropolis with 64 "
+                "chains x one sweep, E_loc and gradients of 64 samples, a 4096^2 x 2048 complex GEMM and a 4096^2 "
+                "eigh; extrapolated to one full step" % cfg["L"])
     if cfg["sampler"] == "mc":
         return ("oracle (numpy FP64 restatement of jVMC) timed on: Metropolis with 256 chains x two sweeps, "
                 "E_loc and gradients of 512 samples, a 4096^2 x 2048 complex GEMM and a 4096^2 eigh; "
@@ -388,6 +406,58 @@ def kernel_bench(args):
             hw = 3.0 * alg
             shape = {"m": m, "n": n, "k": K}
         unit, bound = "TFLOP/s", "tensor"
+    elif args.kernel in ("data", "hermitian", "gemv", "stats"):
+        unit, bound = "GB/s", "hbm"
+        alg = hw = None
+        if args.kernel == "data":
+            # centred O_k -> transposed BF16 hi/lo planes: N=16384, L=64, M=64 (P=4160)
+            N, L, M = 16384, 64, 64
+            P = L * M + M
+            cfg_ = torch.randint(0, 2, (N, L), dtype=torch.int32, device=dev, generator=g)
+            W = (0.05 * torch.randn(L, M, dtype=torch.complex64, device=dev, generator=g)).contiguous()
+            b = (0.05 * torch.randn(M, dtype=torch.complex64, device=dev, generator=g)).contiguous()
+            w = torch.full((N,), 1.0 / N, dtype=torch.float64, device=dev)
+            mean = torch.zeros(P, dtype=torch.complex128, device=dev)
+            hi = torch.empty((2 * P, N), dtype=torch.bfloat16, device=dev)
+            lo = torch.empty_like(hi)
+            fn = lambda: L_.call("vmc_rbm_centered_gradients", 1, L_.ptr(cfg_), N, L, M, L_.ptr(W), L_.ptr(b),
+                                 L_.ptr(w), L_.ptr(mean), 2, L_.ptr(hi), L_.ptr(lo), N, st)
+            nbytes = 2 * (2 * P * N * 2) + N * L * 4 + P * 16 + N * 8
+            shape = {"N": N, "L": L, "M": M, "P": P}
+        elif args.kernel == "hermitian":
+            P = 4096
+            G = torch.randn((2 * P, 2 * P), dtype=torch.float32, device=dev, generator=g)
+            A = torch.empty((P, P), dtype=torch.complex128, device=dev)
+            fn = lambda: L_.call("vmc_gram_to_hermitian", 1, L_.ptr(G), 2 * P, P, 0.0, L_.ptr(A), st)
+            nbytes = 4 * P * P * 4 + P * P * 16   # each needed G entry once (4 per output), A once
+            shape = {"P": P}
+        elif args.kernel == "gemv":
+            P = 8192
+            U = torch.randn((P, P), dtype=torch.complex128, device=dev, generator=g)
+            x = torch.randn(P, dtype=torch.complex128, device=dev, generator=g)
+            y = torch.empty_like(x)
+            wsg = torch.empty(L_.query("vmc_zgemv_workspace_bytes", P), dtype=torch.uint8, device=dev)
+            fn = lambda: (L_.call("vmc_zgemv", 1, L_.ptr(U), P, P, L_.ptr(x), L_.ptr(y), None, 0, st),
+                          L_.call("vmc_zgemv", 0, L_.ptr(U), P, P, L_.ptr(x), L_.ptr(y), L_.ptr(wsg), wsg.numel(), st))
+            nbytes = 2 * (P * P * 16 + 2 * P * 16)   # adjoint and forward product
+            shape = {"P": P, "products": "U^H x and U x"}
+        else:
+            N, L, M = 16384, 64, 256
+            P = L * M + M
+            cfg_ = torch.randint(0, 2, (N, L), dtype=torch.int32, device=dev, generator=g)
+            W = (0.05 * torch.randn(L, M, dtype=torch.complex64, device=dev, generator=g)).contiguous()
+            b = (0.05 * torch.randn(M, dtype=torch.complex64, device=dev, generator=g)).contiguous()
+            w = torch.full((N,), 1.0 / N, dtype=torch.float64, device=dev)
+            E = torch.randn(N, dtype=torch.complex128, device=dev, generator=g)
+            em = torch.zeros(1, dtype=torch.complex128, device=dev)
+            om = torch.empty(P, dtype=torch.complex128, device=dev)
+            fo = torch.empty(P, dtype=torch.complex128, device=dev)
+            ws = torch.empty(L_.query("vmc_rbm_grad_stats_workspace_bytes", N, L, M), dtype=torch.uint8, device=dev)
+            fn = lambda: L_.call("vmc_rbm_grad_stats", 1, L_.ptr(cfg_), N, L, M, L_.ptr(W), L_.ptr(b), L_.ptr(w),
+                                 L_.ptr(E), L_.ptr(em), L_.ptr(om), L_.ptr(fo), L_.ptr(ws), ws.numel(), st)
+            nbytes = N * L * 4 + N * 16 + N * 8 + 2 * P * 16
+            shape = {"N": N, "L": L, "M": M, "P": P}
+            bound = "FP64 reduction (compute)"
     else:
         cfg = WORKLOADS[DEFAULT_WORKLOAD]
         ctx = build(cfg, "mixed")
@@ -415,6 +485,9 @@ def kernel_bench(args):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / args.steps
     out = {"kernel": args.kernel, "ms_per_launch": ms, "shape": shape, "bound": bound}
+    if unit == "GB/s":
+        out["algorithmic_bytes"] = nbytes
+        out["achieved_gbs"] = nbytes / ms / 1e6
     if alg:
         out["algorithmic_tflops"] = alg / ms / 1e9
         out["executed_tflops"] = hw / ms / 1e9
@@ -456,8 +529,25 @@ def quench_bench(args):
         theta = psi.get_parameters()
         t, times, E = 0.0, [], []
         t0 = time.perf_counter()
-        while t < args.quench:
-            theta, dt = st.step(t, td, theta, hamiltonian=H, psi=psi, numSamples=8192)
+
+        # integration error in the metric of S (the norm_fun of the
+        # reference's time-evolution examples: Re v^dagger S v)
+        def s_norm(v):
+            return float(torch.real(torch.vdot(v.to(torch.complex128), td.S_dot(v))))
+
+        class _WallClock(Exception):
+            pass
+
+        def rhs(y, tt, **kw):  # the step-size control may retry: bound the wall clock per RHS
+            if time.perf_counter() - t0 > args.quench_wall:
+                raise _WallClock()
+            return td(y, tt, **kw)
+
+        while t < args.quench and len(E) < args.quench_steps:
+            try:
+                theta, dt = st.step(t, rhs, theta, hamiltonian=H, psi=psi, numSamples=8192, normFunction=s_norm)
+            except _WallClock:
+                break
             psi.set_parameters(theta)
             times.append(t)
             E.append(float(torch.real(td.ElocMean0)))
@@ -465,11 +555,13 @@ def quench_bench(args):
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
         E = np.array(E)
-        res[prec] = {"steps": len(E), "t_end": t, "wall_s": wall, "E0": float(E[0]),
+        res[prec] = {"steps": len(E), "t_end": t, "wall_s": wall, "E0": float(E[0]), "stopped_early": t < args.quench,
                      "drift": float(np.max(np.abs(E - E[0])) / abs(E[0])), "E": E.tolist(), "t": times}
     emit({"metric": "XXZ quench energy drift, mixed vs FP64 solve", "workload": "xxz48_rbm96_quench",
-          "config": {"L": L, "M": M, "delta": delta, "num_samples": 8192, "integrator": "AdaptiveHeun tol 1e-4",
-                     "t_end": args.quench}, "data": "synthetic (seeded)", **res})
+          "config": {"L": L, "M": M, "delta": delta, "num_samples": 8192,
+                     "integrator": "AdaptiveHeun tol 1e-4, S-metric error norm", "t_end": args.quench,
+                     "max_steps": args.quench_steps, "max_wall_s": args.quench_wall},
+          "data": "synthetic (seeded)", **res})
 
 
 def serve_bench(args):
@@ -616,7 +708,7 @@ def main():
            "scaling": "weak", "vs_baseline": None, "dtype": "f32+bf16x3 (FP64 statistics and eigensolve)",
            "data": "synthetic (seeded lattice and parameters)",
            "config": {"workload": args.workload, "precision": args.precision, "num_samples": Ns,
-                      "num_params_complex": P, "l2": "inputs larger than L2 (O_k planes 2.2 GB)",
+                      "num_params_complex": P, "l2": "inputs larger than L2 (O_k bf16 planes %.2f GB)" % (8.0 * P * Ns / 1e9),
                       "parallelism": "replicas" if world > 1 else "single GPU", **cfg},
            "energy": energy, "phase_ms": phases, "gram_kernel_ms": gram_ms, "snr_kernel_ms": snr_ms,
            "roofline": roofline, "clocks": clock, "gpu_launches": launches, "e2e": e2e}

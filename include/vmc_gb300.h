@@ -286,9 +286,12 @@ int vmc_rbm_snr_data(int32_t precision, const int32_t* configs, int64_t num_conf
 int vmc_gram_to_hermitian(int32_t gram_precision, const void* gram, int64_t ld_gram, int32_t num_params,
                           double diag_shift, double* A, vmc_stream_t stream);
 
-/* y = U^H x (adjoint = 1) or y = U x (adjoint = 0); U column-major c128. */
-int vmc_zgemv(int32_t adjoint, const double* U, int64_t ld, int32_t n, const double* x, double* y,
-              vmc_stream_t stream);
+/* y = U^H x (adjoint = 1) or y = U x (adjoint = 0); U column-major c128.
+ * adjoint = 0 needs vmc_zgemv_workspace_bytes(n) of workspace (partial sums
+ * over 256-wide chunks of k, added in a fixed order); adjoint = 1 needs none. */
+size_t vmc_zgemv_workspace_bytes(int32_t n);
+int vmc_zgemv(int32_t adjoint, const double* U, int64_t ld, int32_t n, const double* x, double* y, void* workspace,
+              size_t workspace_bytes, vmc_stream_t stream);
 
 /* The SNR of every eigenvector: snr_k = sqrt(|N |VtF_k|^2 / rhoVar_k|) with
  * rhoVar_k = colsq[k] (+ colsq[n + k] when real_rep), colsq the column sums of
@@ -377,6 +380,95 @@ int vmc_cnn_metropolis(int32_t precision, const vmc_cnn_desc* desc, int32_t* sta
                        const void* params, double mu, uint64_t seed, uint32_t call_index, int64_t therm_steps,
                        int64_t sweep_steps, int64_t samples_per_chain, int32_t* configs_out, void* counters,
                        vmc_stream_t stream);
+
+/* ---------------------------------------------------------------------------
+ * The same statistics and data from materialised log-derivatives O (N, P)
+ * complex128 (compact layout, row stride ld_gradients elements) of any
+ * holomorphic network (e.g. vmc_sym_rbm_gradients output), so that its S/F
+ * build and SNR transform run through the same Gram / eigen / SNR entry
+ * points as the CpxRBM's (stats.py:50-58, 197-205, 255-292; tdvp.py:134-181).
+ * ------------------------------------------------------------------------- */
+size_t vmc_dense_grad_stats_workspace_bytes(int64_t num_configs, int64_t num_params);
+
+/* ok_mean_k = sum_n w_n O_nk, force_k = sum_n w_n conj(O_nk - ok_mean_k)
+ * (E_n - Ebar) = covar(O, E) (fixed-order reductions). */
+int vmc_dense_grad_stats(const double* gradients, int64_t ld_gradients, int64_t num_configs, int64_t num_params,
+                         const double* weights, const double* eloc, const double* eloc_mean, double* ok_mean,
+                         double* force, void* workspace, size_t workspace_bytes, vmc_stream_t stream);
+
+/* X as vmc_rbm_centered_gradients, from O. */
+int vmc_dense_centered_gradients(const double* gradients, int64_t ld_gradients, int64_t num_configs,
+                                 int64_t num_params, const double* weights, const double* ok_mean, int32_t format,
+                                 void* out, void* out_lo, int64_t ld_out, vmc_stream_t stream);
+
+/* H as vmc_rbm_snr_data, from O. */
+int vmc_dense_snr_data(const double* gradients, int64_t ld_gradients, int64_t num_configs, int64_t num_params,
+                       const double* weights, const double* ok_mean, const double* eloc, const double* eloc_mean,
+                       double neg_rhs_re, double neg_rhs_im, const double* force, int32_t format, void* out,
+                       void* out_lo, int64_t ld_out, vmc_stream_t stream);
+
+/* ---------------------------------------------------------------------------
+ * Symmetrised CpxRBM (nets/sym_wrapper.py:22-64 over nets/rbm.py:17-38;
+ * orbits of util/symmetries.py).
+ *
+ * `orbit` (num_sym, L) int32 holds codes 2 * src + flip: site i of the
+ * transformed configuration tau(s) is s[src] (flip 0) or 1 - s[src] (flip 1),
+ * i.e. row i of the reference's orbit matrix o_tau has its one nonzero entry
+ * (+1 or -1) in column src, and tau(s) = (o_tau (2s - 1) + 1) // 2
+ * (sym_wrapper.py:51-54).  `inverse` (num_sym, L) int32 holds, for each site
+ * j, the position i of tau(s) with src = j; the orbit must consist of signed
+ * permutations.  `factor` (num_sym) complex128.
+ * VMC_SYM_EXP: log psi = log sum_tau factor_tau exp(log psi_RBM(tau s)), in
+ * the form of jax.scipy.special.logsumexp(., b=factor) (avgFun_Coefficients_Exp,
+ * sym_wrapper.py:7-9); VMC_SYM_LOG: the mean of log psi_RBM(tau s)
+ * (avgFun_Coefficients_Log, sym_wrapper.py:12-13; factor unused).
+ * Malformed codes or inverse entries make the affected outputs NaN.
+ * ------------------------------------------------------------------------- */
+typedef enum { VMC_SYM_EXP = 0, VMC_SYM_LOG = 1 } vmc_sym_average;
+
+typedef struct {
+  int32_t num_sym;          /* orbit size, 1..4096 */
+  int32_t average;          /* vmc_sym_average */
+  const int32_t* orbit;     /* (num_sym, L) codes */
+  const int32_t* inverse;   /* (num_sym, L) */
+  const double* factor;     /* (num_sym) complex128 */
+} vmc_sym_desc;
+
+/* log psi of the symmetrised net; replaces NQS._eval for a SymNet
+ * (vqs.py:242-251, sym_wrapper.py:48-60).  Output (N) complex128. */
+int vmc_sym_rbm_logpsi(int32_t precision, const int32_t* configs, int64_t num_configs, int32_t num_sites,
+                       int32_t num_hidden, const void* kernel, const void* bias, const vmc_sym_desc* sym,
+                       double* log_psi, vmc_stream_t stream);
+
+/* d log psi / d theta = sum_tau w_tau O_k(tau s), w_tau = factor_tau
+ * psi_RBM(tau s) / psi(s) (Exp) or 1/num_sym (Log); the holomorphic gradient
+ * of sym_wrapper.py:48-60 (flat_gradient_holo, vqs.py:66-69).  Layouts as
+ * vmc_rbm_gradients. */
+int vmc_sym_rbm_gradients(int32_t precision, const int32_t* configs, int64_t num_configs, int32_t num_sites,
+                          int32_t num_hidden, const void* kernel, const void* bias, const vmc_sym_desc* sym,
+                          int32_t layout, double* out, vmc_stream_t stream);
+
+/* O_loc of a branch-free operator for the symmetrised net without forming s'
+ * (Operator.get_O_loc, base.py:162-192): psi(s')/psi(s) = sum_tau w_tau
+ * psi_RBM(tau s') / psi_RBM(tau s), each ratio a product over hidden units
+ * from the tables of vmc_rbm_prepare.  VMC_SYM_EXP only (VMC_ERR_UNSUPPORTED
+ * otherwise).  log_psi_s as vmc_rbm_oloc_fused. */
+int vmc_sym_rbm_oloc_fused(int32_t precision, const int32_t* configs, int64_t num_configs, int32_t num_sites,
+                           int32_t num_hidden, const void* kernel, const void* bias, const void* tables,
+                           const vmc_sym_desc* sym, const vmc_bf_operator* op, const double* log_psi_s,
+                           double* oloc, vmc_stream_t stream);
+
+/* Metropolis sampling of |psi_sym|^mu with single spin flips
+ * (MCSampler._get_samples / _sweep with propose_spin_flip,
+ * sampler.py:264-358); one thread block per chain keeps tanh(theta) of every
+ * orbit element in shared memory (num_sym * num_hidden complex values must
+ * fit, else VMC_ERR_UNSUPPORTED).  Random stream, arguments and outputs as
+ * vmc_rbm_metropolis. */
+int vmc_sym_rbm_metropolis(int32_t precision, int32_t* states, int32_t num_chains, int32_t num_sites,
+                           int32_t num_hidden, const void* kernel, const void* bias, const void* tables,
+                           const vmc_sym_desc* sym, double mu, uint64_t seed, uint32_t call_index,
+                           int64_t therm_steps, int64_t sweep_steps, int64_t samples_per_chain, int32_t* configs_out,
+                           void* counters, vmc_stream_t stream);
 
 #ifdef __cplusplus
 }

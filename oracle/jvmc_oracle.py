@@ -251,6 +251,150 @@ class LookupNet:
 # Variational state (jVMC/vqs.py)
 # ---------------------------------------------------------------------------
 
+# ---------------------------------------------------------------------------
+# Lattice symmetries and the symmetrised network
+# (jVMC/util/symmetries.py, jVMC/nets/sym_wrapper.py)
+# ---------------------------------------------------------------------------
+
+def _perm_matrix(maps_row, idx):
+    o = np.zeros((idx.size, idx.size), dtype=np.int32)
+    o[idx.ravel(), maps_row.ravel()] = 1
+    return o
+
+
+def _unique_orbit(orbits, factors, n):
+    """np.unique over the flattened matrices (rows sorted lexicographically)
+    with the factor of each first occurrence (symmetries.py:142-144, 207-209)."""
+    uo, ind = np.unique(orbits.reshape((-1, n * n)), return_index=True, axis=0)
+    return uo.reshape(-1, n, n), np.asarray(factors)[ind]
+
+
+def get_orbit_1D(L, *args, translation_factor=1., reflection_factor=1., spinflip_factor=1.):
+    """symmetries.py:146-212: orbit matrices (|S|, L, L) and factors."""
+    idx = np.arange(L)
+    refl = {"maps": [idx], "factor": [1.]}
+    trans = {"maps": [idx], "factor": [1.]}
+    if "reflection" in args:
+        refl["maps"].append(idx[::-1])
+        refl["factor"].append(reflection_factor)
+    if "translation" in args:
+        for x in range(1, L):
+            trans["maps"].append(np.roll(idx, x, axis=(0,)))
+            trans["factor"].append(translation_factor ** x)
+    orbits, factors = [], []
+    for mt, ft in zip(trans["maps"], trans["factor"]):
+        for mr, fr in zip(refl["maps"], refl["factor"]):
+            orbits.append(_perm_matrix(mt, idx) @ _perm_matrix(mr, idx))
+            factors.append(ft * fr)
+    orbits = np.array(orbits)
+    factors = np.array(factors)
+    if "spinflip" in args:
+        orbits = np.concatenate([orbits, -orbits], axis=0)
+        factors = np.concatenate([factors, spinflip_factor * factors])
+    return _unique_orbit(orbits, factors, L)
+
+
+def get_orbit_2D_square(L, *args, translation_factor=1., reflection_factor=1., rotation_factor=1.,
+                        spinflip_factor=1.):
+    """symmetries.py:51-148: orbit matrices (|S|, L^2, L^2) and factors."""
+    idx = np.arange(L ** 2).reshape((L, L))
+    rot = {"maps": [idx], "factor": [1.]}
+    refl = {"maps": [idx], "factor": [1.]}
+    trans = {"maps": [idx], "factor": [1.]}
+    if "rotation" in args:
+        rot["maps"] += [idx[::-1, :].T, idx[::-1, ::-1], idx[:, ::-1].T]
+        rot["factor"] += [rotation_factor, rotation_factor ** 2, rotation_factor ** 3]
+    if "reflection" in args:
+        refl["maps"] += [idx[::-1, :], idx[:, ::-1], idx[::-1, ::-1]]
+        refl["factor"] += [reflection_factor, reflection_factor, reflection_factor ** 2]
+    if "translation" in args:
+        for x in range(L):
+            for y in range(L):
+                if x == 0 and y == 0:
+                    continue
+                trans["maps"].append(np.roll(idx, (y, x), axis=(0, 1)))
+                trans["factor"].append(translation_factor ** (x + y))
+    # symmetries.py:134 passes (translation, reflection, rotation) into the
+    # parameters (translation, rotation, reflection) of
+    # get_orbits_from_maps_2D (51-75), whose loops then run over translation,
+    # rotation, reflection and form T @ Rot @ Refl
+    orbits, factors = [], []
+    for mt, ft in zip(trans["maps"], trans["factor"]):
+        for mo, fo in zip(rot["maps"], rot["factor"]):
+            for mr, fr in zip(refl["maps"], refl["factor"]):
+                orbits.append(_perm_matrix(mt, idx) @ _perm_matrix(mo, idx) @ _perm_matrix(mr, idx))
+                factors.append(ft * fo * fr)
+    orbits = np.array(orbits)
+    factors = np.array(factors)
+    if "spinflip" in args:
+        orbits = np.concatenate([orbits, -orbits], axis=0)
+        factors = np.concatenate([factors, spinflip_factor * factors])
+    return _unique_orbit(orbits, factors, L ** 2)
+
+
+def avgFun_Coefficients_Exp(coeffs, factor):
+    """sym_wrapper.py:7-9: logsumexp(coeffs, b=factor) along axis 0 in the
+    form of jax.scipy.special.logsumexp for complex input: terms with
+    factor 0 are dropped, the maximum real part is taken out, and the result
+    is the principal complex log of the scaled sum plus that maximum."""
+    b = np.asarray(factor).reshape((-1,) + (1,) * (coeffs.ndim - 1))
+    a = np.where(b != 0, coeffs, -np.inf)
+    amax = np.max(np.real(a), axis=0)
+    amax = np.where(np.isfinite(amax), amax, 0.0)
+    s = np.sum(np.exp(a - amax) * b, axis=0)
+    return np.log(s.astype(tCpx)) + amax
+
+
+def avgFun_Coefficients_Log(coeffs, factor):
+    """sym_wrapper.py:12-13: mean of the log-coefficients (factor unused)."""
+    return np.mean(coeffs, axis=0)
+
+
+class SymNet:
+    """sym_wrapper.py:22-64: log psi_sym(s) = avgFun_tau(log psi(tau(s)), factor)
+    with tau(s) = (o_tau (2s - 1) + 1) // 2.  The gradient of the holomorphic
+    average is the weighted mean of the per-element gradients, with weights
+    factor_tau exp(log psi(tau s) - log psi_sym(s)) (Exp) or 1/|S| (Log)."""
+
+    def __init__(self, net, orbit, factor, avgFun=avgFun_Coefficients_Exp):
+        self.net = net
+        self.orbit = np.asarray(orbit)
+        self.factor = np.asarray(factor)
+        self.avgFun = avgFun
+        self.holomorphic = net.holomorphic
+        self.realParams = net.realParams
+
+    def leaf_shapes(self, L):
+        return self.net.leaf_shapes(L)
+
+    def transformed(self, s):
+        """(|S|, N, L) configurations tau(s) (sym_wrapper.py:51-54)."""
+        s = np.asarray(s).reshape(np.asarray(s).shape[0], -1)
+        x = 2 * s - 1
+        y = np.einsum("tij,nj->tni", self.orbit, x)
+        return (y + 1) // 2
+
+    def _per_element(self, params, s):
+        ts = self.transformed(s)
+        S, N, L = ts.shape
+        return ts, self.net.apply(params, ts.reshape(S * N, L)).reshape(S, N).astype(tCpx)
+
+    def apply(self, params, s):
+        _, lp = self._per_element(params, s)
+        return self.avgFun(lp, self.factor)
+
+    def grad(self, params, s):
+        ts, lp = self._per_element(params, s)
+        S, N, L = ts.shape
+        if self.avgFun is avgFun_Coefficients_Log:
+            w = np.full((S, N), 1.0 / S, dtype=tCpx)
+        else:
+            lsym = self.apply(params, s)
+            w = self.factor.reshape(S, 1) * np.exp(lp - lsym[None, :])
+        g = self.net.grad(params, ts.reshape(S * N, L))
+        return {k: np.einsum("tn,tnk->nk", w, v.reshape(S, N, -1)) for k, v in g.items()}
+
+
 class NQS:
     """Restatement of vqs.py:115-466 for the nets above.
 

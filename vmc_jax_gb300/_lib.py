@@ -59,7 +59,7 @@ def _ctype(decl):
         inner = base.rstrip("*").strip()
         if inner == "vmc_bf_operator":
             return ctypes.POINTER(BfOperator)
-        if inner == "vmc_cnn_desc":
+        if inner in ("vmc_cnn_desc", "vmc_sym_desc"):
             return ctypes.c_void_p
         if inner == "char":
             return ctypes.c_char_p
@@ -123,10 +123,12 @@ KERNELS_PER_CALL = {
     "vmc_rbm_logpsi": 1, "vmc_rbm_gradients": 1, "vmc_rbm_metropolis": 1, "vmc_bf_matrix_elements": 1,
     "vmc_bf_gather": 1, "vmc_oloc_from_sprimes": 1, "vmc_rbm_oloc_fused": 1, "vmc_weighted_mean_var": 3,
     "vmc_rbm_grad_stats": 3, "vmc_rbm_centered_gradients": 1, "vmc_rbm_snr_data": 1, "vmc_gram_to_hermitian": 1,
-    "vmc_zgemv": 1, "vmc_tdvp_snr": 1, "vmc_tdvp_regularize": 1, "vmc_gram_bf16x3": 1,
+    "vmc_zgemv": 2, "vmc_tdvp_snr": 1, "vmc_tdvp_regularize": 1, "vmc_gram_bf16x3": 1,
     "vmc_gemm_bf16x3_colsq": 2, "vmc_eigvec_bf16x2": 1, "vmc_cnn_logpsi": 1, "vmc_cnn_gradients": 1,
     "vmc_cnn_metropolis": 1, "vmc_rbm_vjp": 4, "vmc_rbm_grad_stats_noalloc": 3,
-    "vmc_rbm_metropolis_devcall": 2,
+    "vmc_rbm_metropolis_devcall": 2, "vmc_sym_rbm_logpsi": 1, "vmc_sym_rbm_gradients": 1,
+    "vmc_sym_rbm_oloc_fused": 1, "vmc_sym_rbm_metropolis": 1, "vmc_dense_grad_stats": 2,
+    "vmc_dense_centered_gradients": 1, "vmc_dense_snr_data": 1,
 }
 launch_count = 0
 
@@ -136,7 +138,10 @@ def call(name, *args):
     global launch_count
     lib = load()
     rc = getattr(lib, name)(*args)
-    launch_count += KERNELS_PER_CALL.get(name, 1)
+    n = KERNELS_PER_CALL.get(name, 1)
+    if name == "vmc_zgemv" and args and args[0]:
+        n = 1  # the adjoint product is one kernel, the plain one two
+    launch_count += n
     if rc != 0:
         msg = lib.vmc_last_error_string().decode(errors="replace")
         raise VmcError(f"{name} failed with status {rc}: {msg}")

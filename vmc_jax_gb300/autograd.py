@@ -9,6 +9,8 @@ log psi] as a function of jVMC's flat real parameter vector theta
   without materialising O (tanh(theta) recomputed from the configurations),
   and d theta = [Re v; -Im v] per leaf, since d log psi / d Re theta_k = O_k
   and d log psi / d Im theta_k = i O_k for a holomorphic net.
+* SymNet(CpxRBM): O (holomorphic, weighted over the orbit) in chunks of
+  at most ``chunk_bytes``, v = conj(g) O, d theta as for the CpxRBM.
 * CNN (real parameters): the backward kernel recomputes every activation of
   each configuration in shared memory; O is formed in chunks of at most
   ``chunk_bytes`` so that N_s x N_p never has to fit in HBM at once.
@@ -19,6 +21,7 @@ import torch
 from . import _lib
 from .nets.cnn import CNN
 from .nets.rbm import CpxRBM
+from .nets.sym_wrapper import SymNet
 
 
 def _flat_configs(psi, configs):
@@ -54,6 +57,20 @@ class _LogPsi(torch.autograd.Function):
             _lib.call("vmc_rbm_vjp", psi.net._prec(psi.precision), _lib.ptr(flat), N, L, M,
                       _lib.ptr(params["kernel"]), _lib.ptr(params.get("bias")), _lib.ptr(g), _lib.ptr(v),
                       _lib.ptr(ws), ws.numel(), _lib.stream())
+            parts, start = [], 0
+            for name, p in params.items():
+                n = p.numel()
+                parts += [v[start:start + n].real, -v[start:start + n].imag]
+                start += n
+            return torch.cat(parts), None, None, None
+        if isinstance(psi.net, SymNet):
+            P = sum(p.numel() for p in params.values())
+            rows = max(1, int(ctx.chunk_bytes // (16 * P)))
+            v = torch.zeros(P, dtype=torch.complex128, device=flat.device)
+            for n0 in range(0, N, rows):
+                O = psi.net.gradients(params, flat[n0:n0 + rows].contiguous(), psi.precision,
+                                      _lib.VMC_GRAD_COMPACT)
+                v += torch.conj(g[n0:n0 + rows]) @ O
             parts, start = [], 0
             for name, p in params.items():
                 n = p.numel()

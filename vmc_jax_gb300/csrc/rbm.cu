@@ -4,21 +4,11 @@
 #include <algorithm>
 
 #include "bf_apply.cuh"
+#include "rbm.cuh"
 #include "reduce.cuh"
 #include "vmc_common.cuh"
 
 namespace vmc {
-
-constexpr int kWarpsPerBlock = 8;
-constexpr int kMaxSites = 4096;
-constexpr int kMaxHidden = 4096;
-
-template <typename T>
-struct rbm_params {
-  const cpx<T>* W;  // (L, M)
-  const cpx<T>* b;  // (M) or null
-  int L, M;
-};
 
 // theta_j = b_j + sum_i (2 s_i - 1) W_ij for the hidden units j = lane + 32 q,
 // written as tanh(theta_j) (want_tanh) or theta_j into `out` (shared).
@@ -174,7 +164,10 @@ __global__ void rbm_oloc_fused_kernel(const int32_t* __restrict__ configs, int64
 
   for (int w = threadIdx.x; w < diagWords; w += blockDim.x) isdiag[w] = 0u;
   __syncthreads();
-  for (int d = threadIdx.x; d < op.num_diag; d += blockDim.x) atomicOr(&isdiag[op.diag[d] >> 5], 1u << (op.diag[d] & 31));
+  for (int d = threadIdx.x; d < op.num_diag; d += blockDim.x) {
+    const int o = op.diag[d];
+    if ((unsigned)o < (unsigned)op.num_ops) atomicOr(&isdiag[o >> 5], 1u << (o & 31));
+  }
   __syncthreads();
 
   const size_t LM = (size_t)p.L * p.M;
@@ -429,16 +422,6 @@ __global__ void rbm_stats_final_kernel(const double2* __restrict__ partial, cons
     okMean[k] = make_double2(mr, mi);
     force[k] = make_double2(fr - cr, fi - ci);
   }
-}
-
-template <typename T>
-rbm_params<T> make_params(const void* kernel, const void* bias, int L, int M) {
-  rbm_params<T> p;
-  p.W = reinterpret_cast<const cpx<T>*>(kernel);
-  p.b = reinterpret_cast<const cpx<T>*>(bias);
-  p.L = L;
-  p.M = M;
-  return p;
 }
 
 int grid_for(int64_t N) {

@@ -13,21 +13,52 @@ namespace vmc {
 // matrix G = R^T R of the real representation R = [Re X | Im X], reading only
 // entries with row <= col (upper tiles), with A[b][a] = conj(A[a][b]) and
 // the diagonal shift A[a][a] *= 1 + shift (tdvp.py:144-145).
+// 32 x 32 output tiles (a0 <= b0 tile pairs): the four G blocks a tile needs
+// are read row-wise (coalesced), the transposed one through shared memory,
+// and A[a][b], A[b][a] = conj(A[a][b]) are both written row-wise.
 template <typename T>
 __global__ void gram_to_hermitian_kernel(const T* __restrict__ G, int64_t ldg, int P, double shift,
                                          double2* __restrict__ A) {
-  const int64_t total = (int64_t)P * P;
-  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-    const int a = (int)(t / P), b = (int)(t - (t / P) * P);
-    const int r = a <= b ? a : b, c = a <= b ? b : a;  // r <= c
-    double re = (double)G[(int64_t)r * ldg + c] + (double)G[(int64_t)(P + r) * ldg + (P + c)];
-    double im = (double)G[(int64_t)r * ldg + (P + c)] - (double)G[(int64_t)c * ldg + (P + r)];
-    if (a > b) im = -im;
-    if (a == b) {
-      im = 0.0;
-      re *= (1.0 + shift);
+  __shared__ double sRe[32][33];
+  __shared__ double sIm[32][33];
+  __shared__ double sT[32][33];
+  const int nt = (P + 31) / 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8 threads
+  for (int tile = blockIdx.x; tile < nt * nt; tile += gridDim.x) {
+    const int ti = tile / nt, tj = tile - (tile / nt) * nt;
+    if (ti > tj) continue;
+    const int a0 = ti * 32, b0 = tj * 32;
+    // sT[b - b0][a - a0] = G[b][P + a]   (row b, contiguous in a)
+    for (int r = ty; r < 32; r += 8) {
+      const int b = b0 + r, a = a0 + tx;
+      sT[r][tx] = (b < P && a < P) ? (double)G[(int64_t)b * ldg + P + a] : 0.0;
     }
-    A[t] = make_double2(re, im);
+    __syncthreads();
+    for (int r = ty; r < 32; r += 8) {
+      const int a = a0 + r, b = b0 + tx;
+      double re = 0.0, im = 0.0;
+      if (a < P && b < P) {
+        // row a, columns b: G[a][b], G[P+a][P+b], G[a][P+b] (all contiguous in b)
+        re = (double)G[(int64_t)a * ldg + b] + (double)G[(int64_t)(P + a) * ldg + P + b];
+        im = (double)G[(int64_t)a * ldg + P + b] - sT[tx][r];
+        if (a == b) {
+          im = 0.0;
+          re *= (1.0 + shift);
+        }
+        A[(int64_t)a * P + b] = make_double2(re, im);
+      }
+      sRe[r][tx] = re;
+      sIm[r][tx] = im;
+    }
+    __syncthreads();
+    if (ti != tj) {
+      // lower tile: A[b][a] = conj(A[a][b]), written row-wise in a
+      for (int r = ty; r < 32; r += 8) {
+        const int b = b0 + r, a = a0 + tx;
+        if (a < P && b < P) A[(int64_t)b * P + a] = make_double2(sRe[tx][r], -sIm[tx][r]);
+      }
+    }
+    __syncthreads();
   }
 }
 
@@ -51,15 +82,33 @@ __global__ void gemv_adjoint_kernel(const double2* __restrict__ U, int64_t ld, i
   }
 }
 
-// y_j = sum_k U_jk x_k ; U column-major: thread per j, k loop (coalesced over j).
-__global__ void gemv_kernel(const double2* __restrict__ U, int64_t ld, int n, const double2* __restrict__ x,
-                            double2* __restrict__ y) {
-  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
-    double re = 0.0, im = 0.0;
-    for (int k = 0; k < n; ++k) {
-      double2 u = U[(int64_t)k * ld + j], v = x[k];
+// y_j = sum_k U_jk x_k ; U column-major.  Grid (j blocks of 256, k chunks):
+// each block sums its k chunk for 256 consecutive j (coalesced), partial
+// results are added in a fixed order by gemv_reduce_kernel.
+constexpr int kGemvChunk = 256;
+__global__ void gemv_partial_kernel(const double2* __restrict__ U, int64_t ld, int n, const double2* __restrict__ x,
+                                    double2* __restrict__ part) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int k0 = blockIdx.y * kGemvChunk;
+  const int k1 = min(n, k0 + kGemvChunk);
+  double re = 0.0, im = 0.0;
+  if (j < n) {
+    for (int k = k0; k < k1; ++k) {
+      const double2 u = U[(int64_t)k * ld + j], v = x[k];
       re += u.x * v.x - u.y * v.y;
       im += u.x * v.y + u.y * v.x;
+    }
+    part[(int64_t)blockIdx.y * n + j] = make_double2(re, im);
+  }
+}
+
+__global__ void gemv_reduce_kernel(const double2* __restrict__ part, int chunks, int n, double2* __restrict__ y) {
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    double re = 0.0, im = 0.0;
+    for (int c = 0; c < chunks; ++c) {
+      const double2 v = part[(int64_t)c * n + j];
+      re += v.x;
+      im += v.y;
     }
     y[j] = make_double2(re, im);
   }
@@ -139,8 +188,8 @@ extern "C" int vmc_gram_to_hermitian(int32_t gram_precision, const void* gram, i
                                      double diag_shift, double* A, vmc_stream_t stream) {
   VMC_REQUIRE(gram && A && num_params > 0 && ld_gram >= 2 * (int64_t)num_params, VMC_ERR_INVALID_ARGUMENT,
               "vmc_gram_to_hermitian: bad arguments");
-  int64_t total = (int64_t)num_params * num_params;
-  int blocks = (int)std::min<int64_t>((total + 255) / 256, 152 * 32);
+  const int64_t nt = ((int64_t)num_params + 31) / 32;
+  int blocks = (int)std::min<int64_t>(nt * nt, 152 * 16);
   if (gram_precision == VMC_F64)
     gram_to_hermitian_kernel<double><<<blocks, 256, 0, as_stream(stream)>>>(
         reinterpret_cast<const double*>(gram), ld_gram, num_params, diag_shift, reinterpret_cast<double2*>(A));
@@ -150,8 +199,12 @@ extern "C" int vmc_gram_to_hermitian(int32_t gram_precision, const void* gram, i
   return check_launch("vmc_gram_to_hermitian");
 }
 
+extern "C" size_t vmc_zgemv_workspace_bytes(int32_t n) {
+  return (size_t)((n + kGemvChunk - 1) / kGemvChunk) * (size_t)n * 16 + 256;
+}
+
 extern "C" int vmc_zgemv(int32_t adjoint, const double* U, int64_t ld, int32_t n, const double* x, double* y,
-                         vmc_stream_t stream) {
+                         void* workspace, size_t workspace_bytes, vmc_stream_t stream) {
   VMC_REQUIRE(U && x && y && n > 0 && ld >= n, VMC_ERR_INVALID_ARGUMENT, "vmc_zgemv: bad arguments");
   if (adjoint) {
     int blocks = (int)std::min<int64_t>(((int64_t)n * 32 + 255) / 256, 152 * 16);
@@ -159,10 +212,17 @@ extern "C" int vmc_zgemv(int32_t adjoint, const double* U, int64_t ld, int32_t n
                                                                reinterpret_cast<const double2*>(x),
                                                                reinterpret_cast<double2*>(y));
   } else {
-    int blocks = (int)std::min<int64_t>(((int64_t)n + 127) / 128, 152 * 16);
-    gemv_kernel<<<blocks, 128, 0, as_stream(stream)>>>(reinterpret_cast<const double2*>(U), ld, n,
-                                                       reinterpret_cast<const double2*>(x),
-                                                       reinterpret_cast<double2*>(y));
+    VMC_REQUIRE(workspace && workspace_bytes >= vmc_zgemv_workspace_bytes(n), VMC_ERR_WORKSPACE,
+                "vmc_zgemv: workspace of %zu bytes needed", vmc_zgemv_workspace_bytes(n));
+    const int chunks = (n + kGemvChunk - 1) / kGemvChunk;
+    dim3 grid((n + 255) / 256, chunks);
+    double2* part = reinterpret_cast<double2*>(workspace);
+    gemv_partial_kernel<<<grid, 256, 0, as_stream(stream)>>>(reinterpret_cast<const double2*>(U), ld, n,
+                                                            reinterpret_cast<const double2*>(x), part);
+    int rc = check_launch("vmc_zgemv(partial)");
+    if (rc) return rc;
+    gemv_reduce_kernel<<<(n + 255) / 256, 256, 0, as_stream(stream)>>>(part, chunks, n,
+                                                                      reinterpret_cast<double2*>(y));
   }
   return check_launch("vmc_zgemv");
 }

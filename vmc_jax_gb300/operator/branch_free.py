@@ -289,12 +289,16 @@ class BranchFreeOperator(Operator):
     # ------------------------------------------------------- fused path
     def fused_capable(self, psi):
         from ..nets.rbm import CpxRBM
+        from ..nets.sym_wrapper import SymNet
+        if isinstance(psi.net, SymNet):
+            return psi.net.average == 0 and self.lDim == 2
         return isinstance(psi.net, CpxRBM) and self.lDim == 2
 
     def get_O_loc_fused(self, samples, psi, logPsiS=None, *args):
-        """O_loc(s) of a CpxRBM state without materialising s': one kernel
-        applies every string and forms psi(s')/psi(s) from tanh(theta) and the
-        exp(+-2W) tables (csrc/rbm.cu).  With ``logPsiS`` given the result is
+        """O_loc(s) of a CpxRBM (or symmetrised CpxRBM) state without
+        materialising s': one kernel applies every string and forms
+        psi(s')/psi(s) from tanh(theta) and the exp(+-2W) tables
+        (csrc/rbm.cu, csrc/sym_rbm.cu).  With ``logPsiS`` given the result is
         relative to it, as in base.py:162-164."""
         s = as_configs(samples)
         psi.init_net(s)
@@ -308,6 +312,12 @@ class BranchFreeOperator(Operator):
         if logPsiS is not None:
             lps = torch.as_tensor(logPsiS).to(device=flat.device, dtype=torch.complex128).reshape(-1).contiguous()
         out = torch.empty(N, dtype=torch.complex128, device=flat.device)
+        from ..nets.sym_wrapper import SymNet
+        if isinstance(psi.net, SymNet):
+            _lib.call("vmc_sym_rbm_oloc_fused", prec, _lib.ptr(flat), N, L, M, _lib.ptr(params["kernel"]),
+                      _lib.ptr(params.get("bias")), _lib.ptr(psi.rbm_tables()),
+                      _lib.ctypes_ref(psi.net.desc(flat.device)), op, _lib.ptr(lps), _lib.ptr(out), _lib.stream())
+            return out.reshape(s.shape[:2])
         _lib.call("vmc_rbm_oloc_fused", prec, _lib.ptr(flat), N, L, M, _lib.ptr(params["kernel"]),
                   _lib.ptr(params.get("bias")), _lib.ptr(psi.rbm_tables()), op, _lib.ptr(lps), _lib.ptr(out),
                   _lib.stream())

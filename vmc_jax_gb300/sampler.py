@@ -2,7 +2,8 @@
 
 ``MCSampler`` runs the Metropolis chains of a CpxRBM in one CUDA kernel
 (one warp per chain, incremental hidden-unit fields, Philox4x32-10 random
-numbers) and keeps the chains on the GPU between calls.  ``ExactSampler``
+numbers; one block per chain for a symmetrised RBM, a full re-evaluation
+per proposal for a CNN) and keeps the chains on the GPU between calls.  ``ExactSampler``
 enumerates the basis and forms the Born weights on the GPU.
 """
 
@@ -73,8 +74,9 @@ class MCSampler:
         # make sure that net is initialised (sampler.py:124)
         self.net(self.states.reshape((1, numChains) + self.sampleShape))
         from .nets.cnn import CNN
-        if not isinstance(self.net.net, (CpxRBM, CNN)):
-            raise NotImplementedError("MCSampler has CUDA kernels for CpxRBM and CNN states")
+        from .nets.sym_wrapper import SymNet
+        if not isinstance(self.net.net, (CpxRBM, CNN, SymNet)):
+            raise NotImplementedError("MCSampler has CUDA kernels for CpxRBM, SymNet(CpxRBM) and CNN states")
         self.logProbFactor = logProbFactor
         self.mu = mu
         self.updateProposer = updateProposer
@@ -138,9 +140,18 @@ class MCSampler:
                       int(self.sweepSteps), int(perChain), _lib.ptr(out), _lib.ptr(self.counters), _lib.stream())
             self.callIndex += 1
             return out.reshape((1, perChain * C) + self.sampleShape)
+        from .nets.sym_wrapper import SymNet
         L, M = psi.net.dims(params)
         out = torch.empty((perChain * C, L), dtype=torch.int32, device=self.states.device)
         self.counters.zero_()
+        if isinstance(psi.net, SymNet):
+            _lib.call("vmc_sym_rbm_metropolis", prec, _lib.ptr(self.states), C, L, M, _lib.ptr(params["kernel"]),
+                      _lib.ptr(params.get("bias")), _lib.ptr(psi.rbm_tables()),
+                      _lib.ctypes_ref(psi.net.desc(self.states.device)), float(self.mu), self.seed,
+                      self.callIndex & 0xFFFFFFFF, int(self.thermalizationSweeps * self.sweepSteps),
+                      int(self.sweepSteps), int(perChain), _lib.ptr(out), _lib.ptr(self.counters), _lib.stream())
+            self.callIndex += 1
+            return out.reshape((1, perChain * C) + self.sampleShape)
         _lib.call("vmc_rbm_metropolis", prec, _lib.ptr(self.states), C, L, M, _lib.ptr(params["kernel"]),
                   _lib.ptr(params.get("bias")), _lib.ptr(psi.rbm_tables()), float(self.mu), self.seed,
                   self.callIndex & 0xFFFFFFFF, int(self.thermalizationSweeps * self.sweepSteps),

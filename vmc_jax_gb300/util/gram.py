@@ -1,5 +1,5 @@
 """Mixed-precision (BF16 x3 split, FP32 accumulation, tcgen05) S build and
-SNR contraction of the TDVP step for a CpxRBM."""
+SNR contraction of the TDVP step for a holomorphic network."""
 
 import torch
 
@@ -13,38 +13,39 @@ def _round_up(x, m):
     return (x + m - 1) // m * m
 
 
-def mixed_hermitian(flat, w, okMean, prec, N, L, M, P, Wk, bk, shift):
+def mixed_hermitian(data, w, okMean, shift):
     """A = <O^dagger O>_c (P x P complex128) from the BF16x3 Gram matrix of the
-    real representation of the centred data."""
-    dev = flat.device
+    real representation of the centred data of ``data`` (a util.sr_data
+    producer)."""
+    dev = data.device
     st = _lib.stream()
+    N, P = data.N, data.P
     ld = _round_up(N, 64)
     R = 2 * P
     hi = torch.empty((R, ld), dtype=torch.bfloat16, device=dev)
     lo = torch.empty((R, ld), dtype=torch.bfloat16, device=dev)
-    _lib.call("vmc_rbm_centered_gradients", prec, _lib.ptr(flat), N, L, M, Wk, bk, _lib.ptr(w), _lib.ptr(okMean),
-              BF16X2, _lib.ptr(hi), _lib.ptr(lo), ld, st)
+    data.centered(w, okMean, BF16X2, hi, lo, ld)
     ldg = _round_up(R, 16)
     G = torch.empty((R, ldg), dtype=torch.float32, device=dev)
     TIMER.mark("gram_kernel")
     _lib.call("vmc_gram_bf16x3", _lib.ptr(hi), _lib.ptr(lo), R, N, ld, _lib.ptr(G), ldg, st)
-    TIMER.mark("gram_kernel_end")
+    TIMER.mark("hermitian")
     del hi, lo
     A = torch.empty((P, P), dtype=torch.complex128, device=dev)
     _lib.call("vmc_gram_to_hermitian", _lib.VMC_F32, _lib.ptr(G), ldg, P, float(shift), _lib.ptr(A), st)
     return A
 
 
-def mixed_snr_colsq(flat, w, okMean, E, emean, f, U, prec, N, L, M, P, Wk, bk, x):
+def mixed_snr_colsq(data, w, okMean, E, emean, f, U, x):
     """Column sums of |H conj(U)|^2 in the real representation (2P floats)."""
-    dev = flat.device
+    dev = data.device
     st = _lib.stream()
+    N, P = data.N, data.P
     R = 2 * P
     ld = _round_up(R, 64)
     hh = torch.empty((N, ld), dtype=torch.bfloat16, device=dev)
     hl = torch.empty((N, ld), dtype=torch.bfloat16, device=dev)
-    _lib.call("vmc_rbm_snr_data", prec, _lib.ptr(flat), N, L, M, Wk, bk, _lib.ptr(w), _lib.ptr(okMean), _lib.ptr(E),
-              _lib.ptr(emean), -x.real, -x.imag, _lib.ptr(f), BF16X2, _lib.ptr(hh), _lib.ptr(hl), ld, st)
+    data.snr_data(w, okMean, E, emean, -complex(x), f, BF16X2, hh, hl, ld)
     bh = torch.empty((R, ld), dtype=torch.bfloat16, device=dev)
     bl = torch.empty((R, ld), dtype=torch.bfloat16, device=dev)
     _lib.call("vmc_eigvec_bf16x2", _lib.ptr(U), U.stride(1), P, _lib.ptr(bh), _lib.ptr(bl), ld, st)
@@ -53,5 +54,5 @@ def mixed_snr_colsq(flat, w, okMean, E, emean, f, U, prec, N, L, M, P, Wk, bk, x
     TIMER.mark("snr_kernel")
     _lib.call("vmc_gemm_bf16x3_colsq", _lib.ptr(hh), _lib.ptr(hl), N, ld, _lib.ptr(bh), _lib.ptr(bl), R, ld, R,
               _lib.ptr(colsq), _lib.ptr(ws), ws.numel(), st)
-    TIMER.mark("snr_kernel_end")
+    TIMER.mark("snr_tail")
     return colsq

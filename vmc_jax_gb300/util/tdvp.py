@@ -1,11 +1,16 @@
 """TDVP solver (mirror of jVMC/util/tdvp.py:26-326).
 
-For a CpxRBM state the right-hand side runs as one GPU pipeline:
+For a CpxRBM (or symmetrised CpxRBM) state the right-hand side runs as one
+GPU pipeline:
 
   sample -> fused O_loc -> FP64 mean/variance of E_loc -> FP64 means of O_k
   and force F -> centred data -> Gram contraction S (FP64 / FP32 / mixed
   BF16x3 on tcgen05) -> FP64 eigendecomposition -> SNR contraction ->
   cutoff loop on the device -> update.
+
+The centred data come from the configurations (CpxRBM: O is never stored)
+or from the materialised O of the network's gradient kernel (SymNet); see
+util/sr_data.py.
 
 The holomorphic ansatz makes the reference's 2P real representation of S
 (tdvp.py:144: makeReal of the 2P x 2P covariance) the real representation
@@ -114,34 +119,36 @@ class TDVP:
     def get_S(self):
         return self.S
 
-    # ================================================= fused CpxRBM path
-    def _rbm_capable(self, psi, hamiltonian):
+    # ========================================== complex (holomorphic) path
+    def _complex_capable(self, psi):
+        """CpxRBM and SymNet(CpxRBM) states take the complex P x P pipeline."""
         from ..nets.rbm import CpxRBM
-        return isinstance(psi.net, CpxRBM) and hasattr(hamiltonian, "fused_capable") and \
-            hamiltonian.fused_capable(psi)
+        from ..nets.sym_wrapper import SymNet
+        return isinstance(psi.net, (CpxRBM, SymNet))
+
+    def _rbm_capable(self, psi, hamiltonian):
+        return self._complex_capable(psi)
 
     def _kernel_precision(self):
         return "fp64" if self.precision == "fp64" else "fp32"
 
     def _rbm_rhs(self, psi, configs, Eloc, p, weights=None):
-        """Everything after E_loc for a CpxRBM; returns the 2P update, the
-        residual and the cutoff (device scalars)."""
+        return self._complex_rhs(psi, configs, Eloc, p, weights)
+
+    def _complex_rhs(self, psi, configs, Eloc, p, weights=None):
+        """Everything after E_loc for a holomorphic state; returns the 2P
+        update, the residual and the cutoff (device scalars)."""
+        from .sr_data import producer
         dev = configs.device
         st = _lib.stream()
         flat = configs.reshape(configs.shape[0] * configs.shape[1], -1)
-        N, L = flat.shape
         w = (p if weights is None else weights).reshape(-1).to(torch.float64).contiguous()
         E = Eloc.reshape(-1).to(torch.complex128).contiguous()
-        kp = self._kernel_precision()
-        params = psi.params_for(kp)
-        prec = psi.net._prec(kp)
-        M = int(params["kernel"].shape[1])
-        hasBias = "bias" in params
-        P = L * M + (M if hasBias else 0)
-        Wk, bk = _lib.ptr(params["kernel"]), _lib.ptr(params.get("bias"))
+        TIMER.mark("statistics")
+        data = producer(psi, flat, self._kernel_precision())
+        N, P = data.N, data.P
 
         # E_loc statistics (stats.py:197-205, 248-252)
-        TIMER.mark("statistics")
         emean = torch.empty(1, dtype=torch.complex128, device=dev)
         evar = torch.empty(1, dtype=torch.float64, device=dev)
         ws = _lib.Workspace.get(_lib.query("vmc_reduce_workspace_bytes", 2))
@@ -150,16 +157,14 @@ class TDVP:
         # mean of O_k and covar(O, E) (stats.py:50-58 via tdvp.py:139)
         okMean = torch.empty(P, dtype=torch.complex128, device=dev)
         covOE = torch.empty(P, dtype=torch.complex128, device=dev)
-        ws = _lib.Workspace.get(_lib.query("vmc_rbm_grad_stats_workspace_bytes", N, L, M))
-        _lib.call("vmc_rbm_grad_stats", prec, _lib.ptr(flat), N, L, M, Wk, bk, _lib.ptr(w), _lib.ptr(E),
-                  _lib.ptr(emean), _lib.ptr(okMean), _lib.ptr(covOE), _lib.ptr(ws), ws.numel(), st)
+        data.stats(w, E, emean, okMean, covOE)
         x = complex(self.rhsPrefactor)
         f = (-x) * covOE                       # complex form of F0 (tdvp.py:139)
 
         # S = <O^dagger O>_c  (tdvp.py:142)
         shift = float(self.diagonalShift) if (self.diagonalShift > 1e-10 and self.makeRealName != 'imag') else 0.0
         TIMER.mark("s_build")
-        A = self._gram(psi, flat, w, okMean, prec, N, L, M, P, Wk, bk, shift)
+        A = self._gram(data, w, okMean, shift)
 
         # eigendecomposition (tdvp.py:153-171), FP64 on the GPU
         TIMER.mark("eigh")
@@ -167,11 +172,13 @@ class TDVP:
         if U.stride(0) != 1:
             U = U.mT.contiguous().mT
         vtf = torch.empty(P, dtype=torch.complex128, device=dev)
-        _lib.call("vmc_zgemv", 1, _lib.ptr(U), U.stride(1), P, _lib.ptr(f), _lib.ptr(vtf), st)
+        ws = _lib.Workspace.get(_lib.query("vmc_zgemv_workspace_bytes", P))
+        _lib.call("vmc_zgemv", 1, _lib.ptr(U), U.stride(1), P, _lib.ptr(f), _lib.ptr(vtf), _lib.ptr(ws), ws.numel(),
+                  st)
 
         # SNR (tdvp.py:173-181)
         TIMER.mark("snr")
-        snr = self._snr(psi, flat, w, okMean, E, emean, f, U, vtf, prec, N, L, M, P, Wk, bk)
+        snr = self._snr(data, w, okMean, E, emean, f, U, vtf)
 
         # regularised pseudo-inverse (tdvp.py:183-213)
         TIMER.mark("solve")
@@ -182,14 +189,51 @@ class TDVP:
                   float(self.pinvCutoff), float(self.pinvTol), float(self.snrTol), _lib.ptr(pinv), _lib.ptr(res), st)
         coef = (pinv.to(torch.complex128) * vtf).contiguous()
         z = torch.empty(P, dtype=torch.complex128, device=dev)
-        _lib.call("vmc_zgemv", 0, _lib.ptr(U), U.stride(1), P, _lib.ptr(coef), _lib.ptr(z), st)
+        ws = _lib.Workspace.get(_lib.query("vmc_zgemv_workspace_bytes", P))
+        _lib.call("vmc_zgemv", 0, _lib.ptr(U), U.stride(1), P, _lib.ptr(coef), _lib.ptr(z), _lib.ptr(ws), ws.numel(),
+                  st)
 
         # bookkeeping in the reference's 2P layout
         self._A, self._shift, self._z, self._covOE = A, shift, z, covOE
+        self._leafSizes = [int(q.numel()) for q in psi.params.values()]
+        self._complexLast = True
         self.ev_c, self.V, self.VtF, self.snr_c = ev, U, vtf, snr
         self.ElocMean = emean[0]
         self.ElocVar = evar[0]
         return self._realrep(psi, z), res[0], res[1]
+
+    def S_dot(self, v):
+        """S0 v (tdvp.py:215-216) for a flat real vector v in the
+        get_parameters layout, S0 = covar(O) of the reference's 2P layout.
+        After the complex path, S0 = [[A, iA], [-iA, A]] per leaf with
+        A = <O^dagger O>_c, so S0 [a; b] = [A z; -i A z] with z = a + i b
+        (A taken without the diagonal shift, as S0 is)."""
+        if not getattr(self, "_complexLast", False):
+            return torch.matmul(self.S0, torch.as_tensor(v, device=self.S0.device).to(self.S0.dtype))
+        v = torch.as_tensor(v, device=self._A.device).to(torch.float64)
+        zs, start = [], 0
+        for n in self._leafSizes:
+            zs.append(torch.complex(v[start:start + n], v[start + n:start + 2 * n]))
+            start += 2 * n
+        z = torch.cat(zs)
+        y = torch.mv(self._A, z)
+        if self._shift:
+            y = y - (self._shift / (1.0 + self._shift)) * self._A.diagonal() * z
+        out, start = [], 0
+        for n in self._leafSizes:
+            yy = y[start:start + n]
+            out += [yy, -1j * yy]
+            start += n
+        return torch.cat(out)
+
+    def get_sr_equation(self, Eloc, gradients):
+        """The TDVP equation with rhsPrefactor 1 (tdvp.py:150-151)."""
+        saved = self.rhsPrefactor
+        self.rhsPrefactor = 1.
+        try:
+            return self.get_tdvp_equation(Eloc, gradients)
+        finally:
+            self.rhsPrefactor = saved
 
     def _realrep(self, psi, z):
         """[Re z_leaf; Im z_leaf] per leaf (get_parameters layout, vqs.py:461-462)."""
@@ -202,36 +246,33 @@ class TDVP:
             start += n
         return torch.cat(parts)
 
-    def _gram(self, psi, flat, w, okMean, prec, N, L, M, P, Wk, bk, shift):
-        dev = flat.device
-        st = _lib.stream()
+    def _gram(self, data, w, okMean, shift):
         if self.precision == "mixed":
             from . import gram as _gram
-            return _gram.mixed_hermitian(flat, w, okMean, prec, N, L, M, P, Wk, bk, shift)
+            return _gram.mixed_hermitian(data, w, okMean, shift)
         fmt, dt = (0, torch.complex128) if self.precision == "fp64" else (1, torch.complex64)
-        X = torch.empty((N, P), dtype=dt, device=dev)
-        _lib.call("vmc_rbm_centered_gradients", prec, _lib.ptr(flat), N, L, M, Wk, bk, _lib.ptr(w),
-                  _lib.ptr(okMean), fmt, _lib.ptr(X), None, P, st)
+        X = torch.empty((data.N, data.P), dtype=dt, device=data.device)
+        data.centered(w, okMean, fmt, X, None, data.P)
         A = torch.matmul(X.mH, X).to(torch.complex128)
         del X
         if shift:
             A.diagonal().mul_(1.0 + shift)
         return A
 
-    def _snr(self, psi, flat, w, okMean, E, emean, f, U, vtf, prec, N, L, M, P, Wk, bk):
-        dev = flat.device
+    def _snr(self, data, w, okMean, E, emean, f, U, vtf):
+        dev = data.device
         st = _lib.stream()
         x = complex(self.rhsPrefactor)
+        P = data.P
         snr = torch.empty(P, dtype=torch.float64, device=dev)
         if self.precision == "mixed":
             from . import gram as _gram
-            colsq = _gram.mixed_snr_colsq(flat, w, okMean, E, emean, f, U, prec, N, L, M, P, Wk, bk, x)
+            colsq = _gram.mixed_snr_colsq(data, w, okMean, E, emean, f, U, x)
             realRep, cprec = 1, _lib.VMC_F32
         else:
             fmt, dt = (0, torch.complex128) if self.precision == "fp64" else (1, torch.complex64)
-            H = torch.empty((N, P), dtype=dt, device=dev)
-            _lib.call("vmc_rbm_snr_data", prec, _lib.ptr(flat), N, L, M, Wk, bk, _lib.ptr(w), _lib.ptr(okMean),
-                      _lib.ptr(E), _lib.ptr(emean), -x.real, -x.imag, _lib.ptr(f), fmt, _lib.ptr(H), None, P, st)
+            H = torch.empty((data.N, P), dtype=dt, device=dev)
+            data.snr_data(w, okMean, E, emean, -x, f, fmt, H, None, P)
             Y = torch.matmul(H, torch.conj(U).to(dt))
             del H
             colsq = (Y.real ** 2 + Y.imag ** 2).sum(0).to(torch.float64).contiguous()
@@ -275,6 +316,7 @@ class TDVP:
     # ===================================================== generic path
     def get_tdvp_equation(self, Eloc, gradients):
         """tdvp.py:134-148 on SampledObs inputs."""
+        self._complexLast = False
         self.ElocMean = Eloc.mean()[0]
         self.ElocVar = Eloc.var()[0]
         self.F0 = (-self.rhsPrefactor) * gradients.covar(Eloc).reshape(-1)
@@ -332,17 +374,24 @@ class TDVP:
         outp = rhsArgs.get("outp", None)
         TIMER.mark("sampling")
         configs, sampleLogPsi, p = self.sampler.sample(numSamples=numSamples)
-        fused = self._rbm_capable(psi, hamiltonian)
+        fused = self._complex_capable(psi)
         if fused:
             TIMER.mark("eloc")
-            Eloc = hamiltonian.get_O_loc_fused(configs, psi, None, t)
-            update, residual, cutoff = self._rbm_rhs(psi, configs, Eloc, p)
+            if hasattr(hamiltonian, "fused_capable") and hamiltonian.fused_capable(psi):
+                Eloc = hamiltonian.get_O_loc_fused(configs, psi, None, t)
+            else:
+                Eloc = hamiltonian.get_O_loc(configs, psi, sampleLogPsi, t)
+            update, residual, cutoff = self._complex_rhs(psi, configs, Eloc, p)
             TIMER.mark("rhs_end")
         else:
+            TIMER.mark("eloc")
             Eloc = hamiltonian.get_O_loc(configs, psi, sampleLogPsi, t)
             EObs = SampledObs(Eloc, p)
+            TIMER.mark("gradients")
             gObs = SampledObs(psi.gradients(configs), p)
+            TIMER.mark("solve")
             update, residual, cutoff = self.solve(EObs, gObs)
+            TIMER.mark("rhs_end")
         psi.set_parameters(tmpParameters)
         if rhsArgs.get("intStep", None) == 0:
             self.ElocMean0 = self.ElocMean
@@ -370,7 +419,7 @@ class TDVP:
         w2 = w2 / w2.sum()
         saved = (self._A, self._shift, self._z, self._covOE, self.ev_c, self.V, self.VtF, self.snr_c,
                  self.ElocMean, self.ElocVar)
-        update1, _, _ = self._rbm_rhs(psi, configs, Eloc, p, weights=w1)
+        update1, _, _ = self._complex_rhs(psi, configs, Eloc, p, weights=w1)
         z1 = self._z
         # tdvp error of update_1 against the full-sample S0, F0 and ElocVar0
         (self._A, self._shift, self._z, self._covOE) = saved[:4]
@@ -381,7 +430,7 @@ class TDVP:
         err1 = torch.abs(1. + (torch.real(torch.vdot(z1, Az1)) - 2. * torch.real(torch.vdot(z1, (-x) * self._covOE)))
                          / self.ElocVar0)
         # residual of update_1 on the odd half: ||S2 u1 - F2|| / ||F2||
-        self._rbm_rhs(psi, configs, Eloc, p, weights=w2)
+        self._complex_rhs(psi, configs, Eloc, p, weights=w2)
         A2, z2shift, cov2 = self._A, self._shift, self._covOE
         r = torch.mv(A2, z1) - (-x) * cov2
         valRes = (torch.linalg.norm(r) / torch.linalg.norm((-x) * cov2)) / residual

@@ -27,11 +27,16 @@ class NQS:
     """Wrapper class providing basic functionality of variational states.
 
     Initializer arguments (vqs.py:115-182):
-        * ``net``: network (``nets.CpxRBM`` or ``nets.CNN``).
+        * ``net``: network (``nets.CpxRBM``, ``nets.CNN`` or
+          ``nets.SymNet`` of a CpxRBM).
         * ``logarithmic``: the net returns log psi (only True is supported).
         * ``batchSize``: kept for interface compatibility; the CUDA kernels
           evaluate any number of configurations in one launch.
         * ``seed``: seed of the parameter initialisation.
+        * ``orbit``: ``util.symmetries.LatticeSymmetry``; wraps ``net`` in a
+          ``SymNet`` (vqs.py:167-168).
+        * ``avgFun``: the SymNet's average (default
+          ``avgFun_Coefficients_Exp``).
         * ``precision``: arithmetic of the network kernels, ``"fp64"``
           (default, the reference's FP64) or ``"fp32"``.
     """
@@ -41,7 +46,8 @@ class NQS:
         if isinstance(net, (list, tuple)):
             raise NotImplementedError("two-network ansatz (TwoNets) has no CUDA path")
         if orbit is not None:
-            raise NotImplementedError("symmetrised networks (SymNet) have no CUDA path")
+            from .nets.sym_wrapper import SymNet, avgFun_Coefficients_Exp
+            net = SymNet(orbit=orbit, net=net, avgFun=avgFun_Coefficients_Exp if avgFun is None else avgFun)
         if not logarithmic:
             raise NotImplementedError("only logarithmic networks are supported")
         _lib.require_cuda()
