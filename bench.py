@@ -17,6 +17,7 @@ bounded sample of the same step, extrapolated to one full step.
 """
 
 import argparse
+import atexit
 import json
 import math
 import os
@@ -174,8 +175,14 @@ class ClockSampler:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
                                           "--format=csv,noheader,nounits", "-lms", "200"],
                                          stdout=self.file, stderr=subprocess.DEVNULL)
+            # the sampler never outlives this process, also when a step raises
+            atexit.register(self._kill)
         except Exception:
             self.proc = None
+
+    def _kill(self):
+        if self.proc is not None and self.proc.poll() is None:
+            self.proc.kill()
 
     def stop(self):
         if self.proc is None:

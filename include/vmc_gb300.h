@@ -374,11 +374,24 @@ int vmc_cnn_logpsi(int32_t precision, const vmc_cnn_desc* desc, const int32_t* c
 int vmc_cnn_gradients(int32_t precision, const vmc_cnn_desc* desc, const int32_t* configs, int64_t num_configs,
                       const void* params, int32_t layout, double* out, vmc_stream_t stream);
 
-/* Metropolis sampling for the CNN with full re-evaluation of each proposal
- * (sampler.py:264-358); random stream and arguments as vmc_rbm_metropolis. */
+/* Metropolis sampling for the CNN (MCSampler._get_samples / _sweep with
+ * propose_spin_flip, sampler.py:264-358): one warp per chain keeps every
+ * layer's activations; a proposal recomputes only the region of each layer
+ * that the flipped site reaches ((l+1)(F-1)+1 sites per dimension for layer
+ * l), with the operations and order of a full evaluation, and accepts iff
+ * u < exp(mu delta log psi).  Random stream and arguments as
+ * vmc_rbm_metropolis. */
 int vmc_cnn_metropolis(int32_t precision, const vmc_cnn_desc* desc, int32_t* states, int32_t num_chains,
                        const void* params, double mu, uint64_t seed, uint32_t call_index, int64_t therm_steps,
                        int64_t sweep_steps, int64_t samples_per_chain, int32_t* configs_out, void* counters,
+                       vmc_stream_t stream);
+
+/* O_loc of a branch-free operator for the CNN without forming s'
+ * (Operator.get_O_loc, base.py:162-192): psi(s')/psi(s) = exp(delta log psi)
+ * from the same local updates (a string flipping n sites: n updates applied
+ * in turn, then undone).  log_psi_s as vmc_rbm_oloc_fused. */
+int vmc_cnn_oloc_fused(int32_t precision, const vmc_cnn_desc* desc, const int32_t* configs, int64_t num_configs,
+                       const void* params, const vmc_bf_operator* op, const double* log_psi_s, double* oloc,
                        vmc_stream_t stream);
 
 /* ---------------------------------------------------------------------------
@@ -401,11 +414,13 @@ int vmc_dense_centered_gradients(const double* gradients, int64_t ld_gradients, 
                                  int64_t num_params, const double* weights, const double* ok_mean, int32_t format,
                                  void* out, void* out_lo, int64_t ld_out, vmc_stream_t stream);
 
-/* H as vmc_rbm_snr_data, from O. */
+/* H as vmc_rbm_snr_data, from O.  real_part != 0 (real-parameter nets,
+ * makeReal = Re): H_nk = sqrt(w_n) (Re((-x) (E_n - Ebar) conj(O_nk -
+ * ok_mean_k)) - Re force_k), imaginary part 0. */
 int vmc_dense_snr_data(const double* gradients, int64_t ld_gradients, int64_t num_configs, int64_t num_params,
                        const double* weights, const double* ok_mean, const double* eloc, const double* eloc_mean,
-                       double neg_rhs_re, double neg_rhs_im, const double* force, int32_t format, void* out,
-                       void* out_lo, int64_t ld_out, vmc_stream_t stream);
+                       double neg_rhs_re, double neg_rhs_im, const double* force, int32_t real_part, int32_t format,
+                       void* out, void* out_lo, int64_t ld_out, vmc_stream_t stream);
 
 /* ---------------------------------------------------------------------------
  * Symmetrised CpxRBM (nets/sym_wrapper.py:22-64 over nets/rbm.py:17-38;

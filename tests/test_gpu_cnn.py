@@ -109,3 +109,111 @@ def test_cnn_tdvp_exact(cuda):
     uo = tdo(opsi.get_parameters(), 0., psi=opsi, hamiltonian=Ho, intStep=0)
     assert abs(complex(td.ElocMean0) - tdo.ElocMean0) / abs(tdo.ElocMean0) < 1e-10
     assert _rel(u, uo) < 1e-8
+    md, mdo = td.get_metadata(), tdo.metaData
+    assert _rel(md["spectrum"].cpu().numpy(), mdo["spectrum"]) < 1e-8
+    v = np.random.default_rng(0).normal(size=u.size)
+    assert _rel(td.S_dot(torch.as_tensor(v, device=cuda)).cpu().numpy(), tdo.S0 @ v) < 1e-10
+
+
+def _tfim2d(V, n, h):
+    H = V.operator.BranchFreeOperator()
+    for y in range(n):
+        for x in range(n):
+            i = n * y + x
+            H.add(V.operator.scal_opstr(-1.0, (V.operator.Sz(i), V.operator.Sz(n * y + (x + 1) % n))))
+            H.add(V.operator.scal_opstr(-1.0, (V.operator.Sz(i), V.operator.Sz(n * ((y + 1) % n) + x))))
+            H.add(V.operator.scal_opstr(-h, (V.operator.Sx(i),)))
+    return H
+
+
+def test_cnn_tdvp_mc_snr(cuda):
+    """MCSampler (same Philox chains on both sides) + SNR regulariser for the
+    real-parameter CNN: update 1e-8, SNR 1e-6 relative (FP64)."""
+    import vmc_jax_gb300 as V
+    psi, opsi = _pair((4, 4), (3, 3), (3, 2), seed=12, scale=0.3)
+    H = _tfim2d(V, 4, 3.0)
+    Ho = O.tfim(16, 1.0, 3.0, lattice=(4, 4))
+    mc = V.sampler.MCSampler(psi, (4, 4), 31, updateProposer=V.sampler.propose_spin_flip, numChains=64,
+                             numSamples=1024, thermalizationSweeps=2, sweepSteps=16)
+    mco = O.MCSampler(opsi, (4, 4), 31, numChains=64, numSamples=1024, thermalizationSweeps=2, sweepSteps=16)
+    td = V.util.TDVP(mc, makeReal="real", rhsPrefactor=1., snrTol=2)
+    tdo = O.TDVP(mco, makeReal="real", rhsPrefactor=1., snrTol=2)
+    u = td(psi.get_parameters(), 0., psi=psi, hamiltonian=H, intStep=0).cpu().numpy()
+    uo = tdo(opsi.get_parameters(), 0., psi=opsi, hamiltonian=Ho, intStep=0)
+    assert abs(complex(td.ElocMean0) - tdo.ElocMean0) / abs(tdo.ElocMean0) < 1e-10
+    assert _rel(u, uo) < 1e-8
+    assert _rel(td.get_snr().cpu().numpy(), tdo.metaData["SNR"]) < 1e-6
+
+
+@pytest.mark.parametrize("precision", ["fp32", "mixed"])
+def test_cnn_tdvp_reduced_precision(cuda, precision):
+    """FP32 / mixed S and SNR builds against FP64 on the same samples."""
+    import vmc_jax_gb300 as V
+    H = _tfim2d(V, 4, 3.0)
+    out = {}
+    for prec in ("fp64", precision):
+        psi, _ = _pair((4, 4), (3, 3), (3, 2), seed=13, scale=0.3)
+        mc = V.sampler.MCSampler(psi, (4, 4), 8, updateProposer=V.sampler.propose_spin_flip, numChains=128,
+                                 numSamples=4096, thermalizationSweeps=2, sweepSteps=16)
+        configs, lp, p = mc.sample()
+        psi.precision = "fp64" if prec == "fp64" else "fp32"
+        psi._touch()
+        td = V.util.TDVP(mc, makeReal="real", rhsPrefactor=1., snrTol=2, precision=prec)
+        Eloc = H.get_O_loc(configs, psi, lp)
+        upd, _, _ = td._complex_rhs(psi, configs, Eloc, p)
+        out[prec] = (upd.cpu().numpy(), complex(td.ElocMean))
+    (u64, e64), (u, e) = out["fp64"], out[precision]
+    assert abs(e - e64) / abs(e64) < 1e-5
+    # the regularised solve amplifies the ~1e-6 relative error of the BF16x3
+    # S by its conditioning (update 2e-3 relative for these weights)
+    assert _rel(u, u64) < (1e-3 if precision == "fp32" else 1e-2)
+
+
+def _xxz2d(V, n, delta):
+    H = V.operator.BranchFreeOperator()
+    for y in range(n):
+        for x in range(n):
+            i = n * y + x
+            for j in (n * y + (x + 1) % n, n * ((y + 1) % n) + x):
+                H.add(V.operator.scal_opstr(1.0, (V.operator.Sx(i), V.operator.Sx(j))))
+                H.add(V.operator.scal_opstr(1.0, (V.operator.Sy(i), V.operator.Sy(j))))
+                H.add(V.operator.scal_opstr(delta, (V.operator.Sz(i), V.operator.Sz(j))))
+    return H
+
+
+@pytest.mark.parametrize("model", ["tfim", "xxz"])
+@pytest.mark.parametrize("shape,F,channels", [((4, 4), (3, 3), (3, 2)), ((10, 10), (3, 3), (8, 8)),
+                                              ((3, 3), (3, 3), (2, 2, 2))])
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_cnn_fused_oloc(cuda, model, shape, F, channels, precision):
+    """Fused E_loc from local updates of the activations (one- and two-flip
+    strings) against the oracle's s' expansion; also relative to a given
+    log psi(s)."""
+    import vmc_jax_gb300 as V
+    if model == "xxz" and shape != (4, 4):
+        pytest.skip("two-flip strings checked on the 4x4 lattice")
+    psi, opsi = _pair(shape, F, channels, seed=21, scale=0.3)
+    n = shape[0]
+    if model == "tfim":
+        H = _tfim2d(V, n, 3.0)
+        Ho = O.tfim(n * n, 1.0, 3.0, lattice=shape)
+    else:
+        H = _xxz2d(V, n, 1.5)
+        Ho = O.BranchFreeOperator()
+        for y in range(n):
+            for x in range(n):
+                i = n * y + x
+                for j in (n * y + (x + 1) % n, n * ((y + 1) % n) + x):
+                    Ho.add(O.scal_opstr(1.0, (O.Sx(i), O.Sx(j))))
+                    Ho.add(O.scal_opstr(1.0, (O.Sy(i), O.Sy(j))))
+                    Ho.add(O.scal_opstr(1.5, (O.Sz(i), O.Sz(j))))
+    s = np.random.default_rng(22).integers(0, 2, (1, 120) + shape).astype(np.int32)
+    psi.precision = precision
+    psi._touch()
+    assert H.fused_capable(psi)
+    ref = Ho.get_O_loc(s, opsi)
+    tol = 1e-11 if precision == "fp64" else 2e-4
+    assert _rel(H.get_O_loc(s, psi).cpu().numpy(), ref) < tol
+    lp = opsi(s) + 0.25 - 0.1j
+    got = H.get_O_loc(s, psi, torch.as_tensor(lp, device=cuda)).cpu().numpy()
+    assert _rel(got, Ho.get_O_loc(s, opsi, lp)) < tol

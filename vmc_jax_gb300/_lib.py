@@ -128,7 +128,7 @@ KERNELS_PER_CALL = {
     "vmc_cnn_metropolis": 1, "vmc_rbm_vjp": 4, "vmc_rbm_grad_stats_noalloc": 3,
     "vmc_rbm_metropolis_devcall": 2, "vmc_sym_rbm_logpsi": 1, "vmc_sym_rbm_gradients": 1,
     "vmc_sym_rbm_oloc_fused": 1, "vmc_sym_rbm_metropolis": 1, "vmc_dense_grad_stats": 2,
-    "vmc_dense_centered_gradients": 1, "vmc_dense_snr_data": 1,
+    "vmc_dense_centered_gradients": 1, "vmc_dense_snr_data": 1, "vmc_cnn_oloc_fused": 1,
 }
 launch_count = 0
 

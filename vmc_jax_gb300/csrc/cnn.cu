@@ -8,6 +8,7 @@
 // them instead of storing activations per sample in HBM.
 #include <algorithm>
 
+#include "bf_apply.cuh"
 #include "vmc_common.cuh"
 
 namespace vmc {
@@ -231,59 +232,6 @@ __global__ void cnn_grad_kernel(const int32_t* __restrict__ configs, int64_t N, 
 
 namespace vmc {
 
-// Metropolis for the CNN: one warp per chain, single-flip proposals, full
-// re-evaluation of log psi(s') (sampler.py:325-358), same Philox stream and
-// decision rule as the RBM sampler.
-template <typename T>
-__global__ void cnn_metropolis_kernel(int32_t* __restrict__ states, int C, cnn_geom g, const T* __restrict__ prm,
-                                      int warps, double mu, uint64_t seed, uint32_t call, int64_t thermSteps,
-                                      int64_t sweepSteps, int64_t samplesPerChain, int32_t* __restrict__ configsOut,
-                                      unsigned long long* __restrict__ counters) {
-  extern __shared__ unsigned char smem[];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int chain = blockIdx.x * warps + warp;
-  if (chain >= C) return;
-  const size_t zBytes = (size_t)g.layers * g.sites * g.maxC * sizeof(T);
-  const size_t per = (zBytes + 2 * g.sites + 15) & ~(size_t)15;
-  T* z = reinterpret_cast<T*>(smem + warp * per);
-  int8_t* cfg = reinterpret_cast<int8_t*>(smem + warp * per + zBytes);
-  int8_t* prop = cfg + g.sites;
-  int32_t* st = states + (size_t)chain * g.sites;
-  for (int i = lane; i < g.sites; i += 32) cfg[i] = (int8_t)st[i];
-  __syncwarp();
-  warp_forward(g, prm, cfg, z, lane);
-  double cur = (double)warp_output(g, z, lane);
-  cur = __shfl_sync(0xffffffffu, cur, 0);
-  unsigned long long accepted = 0;
-  const int64_t total = thermSteps + sweepSteps * samplesPerChain;
-  for (int64_t step = 0; step < total; ++step) {
-    const mc_draw d = metropolis_draw(seed, call, (uint32_t)step, (uint32_t)chain, g.sites);
-    for (int i = lane; i < g.sites; i += 32) prop[i] = i == d.site ? (int8_t)(1 - cfg[i]) : cfg[i];
-    __syncwarp();
-    warp_forward(g, prm, prop, z, lane);
-    double nw = (double)warp_output(g, z, lane);
-    nw = __shfl_sync(0xffffffffu, nw, 0);
-    const double P = exp(mu * nw - mu * cur);
-    if (d.u64() < P) {
-      if (lane == 0) cfg[d.site] = (int8_t)(1 - cfg[d.site]);
-      cur = nw;
-      ++accepted;
-    }
-    __syncwarp();
-    if (step >= thermSteps && ((step - thermSteps + 1) % sweepSteps) == 0) {
-      const int64_t s = (step - thermSteps + 1) / sweepSteps - 1;
-      int32_t* o = configsOut + ((size_t)s * C + chain) * g.sites;
-      for (int k = lane; k < g.sites; k += 32) o[k] = cfg[k];
-    }
-  }
-  __syncwarp();
-  for (int k = lane; k < g.sites; k += 32) st[k] = cfg[k];
-  if (lane == 0) {
-    atomicAdd(&counters[0], (unsigned long long)total);
-    atomicAdd(&counters[1], accepted);
-  }
-}
-
 static int make_geom(const vmc_cnn_desc* d, cnn_geom& g) {
   VMC_REQUIRE(d, VMC_ERR_INVALID_ARGUMENT, "cnn: null descriptor");
   VMC_REQUIRE((d->ndim == 1 || d->ndim == 2) && d->num_layers >= 1 && d->num_layers <= kCnnMaxLayers,
@@ -339,6 +287,355 @@ static int pick_warps(size_t perWarp, int maxWarps, const char* fn) {
 template <typename K>
 static void allow_smem(K* fn, size_t bytes) {
   if (bytes > 48 * 1024) cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+// ------------------------------------------------------------ local updates
+// A flip of site q0 changes the outputs of layer l (0-based) only on the
+// square of (l+1)(F-1)+1 sites ending at q0 (output p reads p .. p+F-1), so
+// a proposal recomputes those regions from the stored activations of the
+// layer below (the region of layer l-1 taken from the proposal, the rest
+// from the chain's state) and the change of log psi is the sum of the last
+// layer's activation changes.  Every region value is formed with the same
+// operations in the same order as the full forward pass, so an accepted
+// proposal leaves exactly the activations of a full evaluation.
+struct cnn_local {
+  int h[kCnnMaxLayers], w[kCnnMaxLayers];  // region extents (capped at the lattice)
+  int aOff[kCnnMaxLayers];                 // activations of layer l: S x ch[l]
+  int newOff[kCnnMaxLayers];               // region values of layer l: h w x ch[l]
+  int winOff;                              // input window of the current layer
+  int perWarp;                             // elements per warp
+};
+
+static cnn_local make_local(const cnn_geom& g) {
+  cnn_local lc;
+  int off = 0;
+  for (int l = 0; l < kCnnMaxLayers; ++l) {
+    lc.aOff[l] = 0;
+    lc.newOff[l] = 0;
+    lc.h[l] = lc.w[l] = 1;
+  }
+  for (int l = 0; l < g.layers; ++l) {
+    lc.aOff[l] = off;
+    off += g.sites * g.ch[l];
+  }
+  int win = 0;
+  for (int l = 0; l < g.layers; ++l) {
+    lc.h[l] = std::min(g.H, (l + 1) * (g.FH - 1) + 1);
+    lc.w[l] = std::min(g.W, (l + 1) * (g.FW - 1) + 1);
+    lc.newOff[l] = off;
+    off += lc.h[l] * lc.w[l] * g.ch[l];
+    if (l > 0) win = std::max(win, (lc.h[l] + g.FH - 1) * (lc.w[l] + g.FW - 1) * g.ch[l - 1]);
+  }
+  lc.winOff = off;
+  off += win;
+  lc.perWarp = off;
+  return lc;
+}
+
+__device__ __forceinline__ int wrap(int v, int n) {
+  v %= n;
+  return v < 0 ? v + n : v;
+}
+
+// activations of every layer of cfg into a (one warp)
+template <typename T>
+__device__ T warp_forward_act(const cnn_geom& g, const cnn_local& lc, const T* prm, const int8_t* cfg, T* a,
+                              int lane) {
+  const int S = g.sites;
+  for (int l = 0; l < g.layers; ++l) {
+    const int cin = l == 0 ? 1 : g.ch[l - 1], cout = g.ch[l];
+    const T* K = prm + g.kOff[l];
+    const T* in = a + lc.aOff[l > 0 ? l - 1 : 0];
+    T* o_ = a + lc.aOff[l];
+    for (int o = lane; o < S * cout; o += 32) {
+      const int p = o / cout, c = o - p * cout;
+      const int y = p / g.W, x = p - y * g.W;
+      T acc = g.bOff[l] >= 0 ? prm[g.bOff[l] + c] : T(0);
+      for (int dy = 0; dy < g.FH; ++dy) {
+        int yy = y + dy;
+        if (yy >= g.H) yy -= g.H;
+        for (int dx = 0; dx < g.FW; ++dx) {
+          int xx = x + dx;
+          if (xx >= g.W) xx -= g.W;
+          const int q = yy * g.W + xx;
+          const T* kk = K + ((size_t)(dy * g.FW + dx) * cin) * cout + c;
+          if (l == 0) {
+            acc += (cfg[q] ? T(1) : T(-1)) * kk[0];
+          } else {
+            for (int ci = 0; ci < cin; ++ci) acc += in[(size_t)q * cin + ci] * kk[(size_t)ci * cout];
+          }
+        }
+      }
+      o_[o] = act_f(g.act[l], acc);
+    }
+    __syncwarp();
+  }
+  const int cl = g.ch[g.layers - 1];
+  const T* al = a + lc.aOff[g.layers - 1];
+  T s = T(0);
+  for (int o = lane; o < S * cl; o += 32) s += al[o];
+  s = warp_sum(s);
+  return s / sqrt(T(S * cl));
+}
+
+__device__ __forceinline__ void region_origin(const cnn_geom& g, const cnn_local& lc, int l, int qy, int qx, int& y0,
+                                              int& x0) {
+  y0 = lc.h[l] == g.H ? 0 : wrap(qy - (l + 1) * (g.FH - 1), g.H);
+  x0 = lc.w[l] == g.W ? 0 : wrap(qx - (l + 1) * (g.FW - 1), g.W);
+}
+
+// change of log psi for flipping site q0 of cfg; the region values stay in
+// the warp's scratch for warp_local_commit (one warp, all lanes return it)
+template <typename T>
+__device__ T warp_local_delta(const cnn_geom& g, const cnn_local& lc, const T* prm, const int8_t* cfg, const T* a,
+                              T* scr, int q0, int lane) {
+  const int qy = q0 / g.W, qx = q0 - (q0 / g.W) * g.W;
+  for (int l = 0; l < g.layers; ++l) {
+    const int cin = l == 0 ? 1 : g.ch[l - 1], cout = g.ch[l];
+    const int h = lc.h[l], w = lc.w[l];
+    int y0, x0;
+    region_origin(g, lc, l, qy, qx, y0, x0);
+    const T* K = prm + g.kOff[l];
+    T* nl = scr + lc.newOff[l];
+    const int WW = w + g.FW - 1;
+    T* win = scr + lc.winOff;
+    if (l > 0) {
+      // inputs of this layer's region: layer l-1 on the rectangle starting at (y0, x0)
+      const int hp = lc.h[l - 1], wp = lc.w[l - 1];
+      int y0p, x0p;
+      region_origin(g, lc, l - 1, qy, qx, y0p, x0p);
+      const int WH = h + g.FH - 1;
+      const T* np = scr + lc.newOff[l - 1];
+      const T* ap = a + lc.aOff[l - 1];
+      for (int o = lane; o < WH * WW * cin; o += 32) {
+        const int cell = o / cin, ci = o - cell * cin;
+        const int wy = cell / WW, wx = cell - wy * WW;
+        const int sy = wrap(y0 + wy, g.H), sx = wrap(x0 + wx, g.W);
+        const int dy = wrap(sy - y0p, g.H), dx = wrap(sx - x0p, g.W);
+        win[o] = (dy < hp && dx < wp) ? np[(dy * wp + dx) * cin + ci] : ap[(size_t)(sy * g.W + sx) * cin + ci];
+      }
+      __syncwarp();
+    }
+    for (int o = lane; o < h * w * cout; o += 32) {
+      const int cell = o / cout, c = o - cell * cout;
+      const int ry = cell / w, rx = cell - ry * w;
+      T acc = g.bOff[l] >= 0 ? prm[g.bOff[l] + c] : T(0);
+      if (l == 0) {
+        const int py = wrap(y0 + ry, g.H), px = wrap(x0 + rx, g.W);
+        for (int dy = 0; dy < g.FH; ++dy) {
+          int yy = py + dy;
+          if (yy >= g.H) yy -= g.H;
+          for (int dx = 0; dx < g.FW; ++dx) {
+            int xx = px + dx;
+            if (xx >= g.W) xx -= g.W;
+            const int q = yy * g.W + xx;
+            const int sv = cfg[q] ^ (q == q0 ? 1 : 0);
+            acc += (sv ? T(1) : T(-1)) * K[(size_t)(dy * g.FW + dx) * cout + c];
+          }
+        }
+      } else {
+        for (int dy = 0; dy < g.FH; ++dy)
+          for (int dx = 0; dx < g.FW; ++dx) {
+            const T* in = win + (size_t)((ry + dy) * WW + (rx + dx)) * cin;
+            const T* kk = K + ((size_t)(dy * g.FW + dx) * cin) * cout + c;
+            for (int ci = 0; ci < cin; ++ci) acc += in[ci] * kk[(size_t)ci * cout];
+          }
+      }
+      nl[o] = act_f(g.act[l], acc);
+    }
+    __syncwarp();
+  }
+  const int l = g.layers - 1, cout = g.ch[l], w = lc.w[l];
+  int y0, x0;
+  region_origin(g, lc, l, qy, qx, y0, x0);
+  const T* nl = scr + lc.newOff[l];
+  const T* al = a + lc.aOff[l];
+  T s = T(0);
+  for (int o = lane; o < lc.h[l] * w * cout; o += 32) {
+    const int cell = o / cout, c = o - cell * cout;
+    const int ry = cell / w, rx = cell - ry * w;
+    const int site = wrap(y0 + ry, g.H) * g.W + wrap(x0 + rx, g.W);
+    s += nl[o] - al[(size_t)site * cout + c];
+  }
+  s = warp_sum(s);
+  return s / sqrt(T(g.sites * cout));
+}
+
+// the region values of the last warp_local_delta become the state; cfg[q0]
+// flips (one warp)
+template <typename T>
+__device__ void warp_local_commit(const cnn_geom& g, const cnn_local& lc, int8_t* cfg, T* a, const T* scr, int q0,
+                                  int lane) {
+  const int qy = q0 / g.W, qx = q0 - (q0 / g.W) * g.W;
+  for (int l = 0; l < g.layers; ++l) {
+    const int cout = g.ch[l], w = lc.w[l];
+    int y0, x0;
+    region_origin(g, lc, l, qy, qx, y0, x0);
+    const T* nl = scr + lc.newOff[l];
+    T* al = a + lc.aOff[l];
+    for (int o = lane; o < lc.h[l] * w * cout; o += 32) {
+      const int cell = o / cout, c = o - cell * cout;
+      const int ry = cell / w, rx = cell - ry * w;
+      const int site = wrap(y0 + ry, g.H) * g.W + wrap(x0 + rx, g.W);
+      al[(size_t)site * cout + c] = nl[o];
+    }
+  }
+  __syncwarp();
+  if (lane == 0) cfg[q0] = (int8_t)(1 - cfg[q0]);
+  __syncwarp();
+}
+
+// parameters in shared memory when they fit (staged by the whole block)
+template <typename T>
+__device__ const T* stage_params(const T* __restrict__ prm, int P, T* dst, bool fits) {
+  if (!fits) return prm;
+  for (int k = threadIdx.x; k < P; k += blockDim.x) dst[k] = prm[k];
+  __syncthreads();
+  return dst;
+}
+
+constexpr int kCnnParamSmem = 32 * 1024;
+
+// Metropolis with local updates: one warp per chain, same Philox stream and
+// decision rule (u < exp(mu * delta log psi)) as the RBM sampler.
+template <typename T>
+__global__ void cnn_metropolis_local_kernel(int32_t* __restrict__ states, int C, const __grid_constant__ cnn_geom g,
+                                            const __grid_constant__ cnn_local lc,
+                                            const T* __restrict__ prmG, int warps, bool prmInSmem, double mu,
+                                            uint64_t seed, uint32_t call, int64_t thermSteps, int64_t sweepSteps,
+                                            int64_t samplesPerChain, int32_t* __restrict__ configsOut,
+                                            unsigned long long* __restrict__ counters) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const size_t prmBytes = prmInSmem ? (((size_t)g.P * sizeof(T) + 15) & ~(size_t)15) : 0;
+  const T* prm = stage_params(prmG, g.P, reinterpret_cast<T*>(smem), prmInSmem);
+  const size_t per = ((size_t)lc.perWarp * sizeof(T) + g.sites + 15) & ~(size_t)15;
+  T* a = reinterpret_cast<T*>(smem + prmBytes + warp * per);
+  T* scr = a;  // scratch offsets follow the activations inside the same per-warp block
+  int8_t* cfg = reinterpret_cast<int8_t*>(a + lc.perWarp);
+  const int chain = blockIdx.x * warps + warp;
+  if (chain >= C) return;  // after the block-wide staging; whole warps exit together
+  int32_t* st = states + (size_t)chain * g.sites;
+  for (int i = lane; i < g.sites; i += 32) cfg[i] = (int8_t)st[i];
+  __syncwarp();
+  warp_forward_act(g, lc, prm, cfg, a, lane);
+  unsigned long long accepted = 0;
+  const int64_t total = thermSteps + sweepSteps * samplesPerChain;
+  for (int64_t step = 0; step < total; ++step) {
+    const mc_draw d = metropolis_draw(seed, call, (uint32_t)step, (uint32_t)chain, g.sites);
+    const T delta = warp_local_delta(g, lc, prm, cfg, a, scr, d.site, lane);
+    const double P = exp(mu * (double)delta);
+    if (d.u64() < P) {
+      warp_local_commit(g, lc, cfg, a, scr, d.site, lane);
+      ++accepted;
+    }
+    if (step >= thermSteps && ((step - thermSteps + 1) % sweepSteps) == 0) {
+      const int64_t s = (step - thermSteps + 1) / sweepSteps - 1;
+      int32_t* o = configsOut + ((size_t)s * C + chain) * g.sites;
+      for (int k = lane; k < g.sites; k += 32) o[k] = cfg[k];
+    }
+  }
+  __syncwarp();
+  for (int k = lane; k < g.sites; k += 32) st[k] = cfg[k];
+  if (lane == 0) {
+    atomicAdd(&counters[0], (unsigned long long)total);
+    atomicAdd(&counters[1], accepted);
+  }
+}
+
+// O_loc without materialising s' (Operator.get_O_loc, base.py:162-192): one
+// warp per configuration; lane k applies string c0 + k; a one-flip string
+// costs one local update, a string flipping n sites n local updates applied
+// in turn and n more to restore the state.
+template <typename T>
+__global__ void cnn_oloc_fused_kernel(const int32_t* __restrict__ configs, int64_t N, const __grid_constant__ cnn_geom g,
+                                      const __grid_constant__ cnn_local lc,
+                                      const T* __restrict__ prmG, int warps, bool prmInSmem,
+                                      const __grid_constant__ vmc_bf_operator op,
+                                      const double2* __restrict__ logPsiS, double2* __restrict__ out) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const size_t prmBytes = prmInSmem ? (((size_t)g.P * sizeof(T) + 15) & ~(size_t)15) : 0;
+  const T* prm = stage_params(prmG, g.P, reinterpret_cast<T*>(smem), prmInSmem);
+  const int diagWords = (op.num_ops + 31) >> 5;
+  uint32_t* isdiag = reinterpret_cast<uint32_t*>(smem + prmBytes);
+  const size_t diagBytes = ((size_t)diagWords * 4 + 15) & ~(size_t)15;
+  const int nw = (g.sites + 31) >> 5;
+  const size_t per = ((size_t)lc.perWarp * sizeof(T) + (size_t)nw * 4 + g.sites + 32 * VMC_BF_MAX_LEN * 2 + 15) &
+                     ~(size_t)15;
+  unsigned char* base = smem + prmBytes + diagBytes + warp * per;
+  T* a = reinterpret_cast<T*>(base);
+  T* scr = a;
+  uint32_t* occ = reinterpret_cast<uint32_t*>(a + lc.perWarp);
+  int16_t* fsRow = reinterpret_cast<int16_t*>(occ + nw);
+  int8_t* cfg = reinterpret_cast<int8_t*>(fsRow + 32 * VMC_BF_MAX_LEN);
+  for (int w = threadIdx.x; w < diagWords; w += blockDim.x) isdiag[w] = 0u;
+  __syncthreads();
+  for (int d = threadIdx.x; d < op.num_diag; d += blockDim.x) {
+    const int o = op.diag[d];
+    if ((unsigned)o < (unsigned)op.num_ops) atomicOr(&isdiag[o >> 5], 1u << (o & 31));
+  }
+  __syncthreads();
+  for (int64_t n = (int64_t)blockIdx.x * warps + warp; n < N; n += (int64_t)gridDim.x * warps) {
+    warp_load_config(configs + n * g.sites, g.sites, cfg, occ, lane);
+    const T lpNet = warp_forward_act(g, lc, prm, cfg, a, lane);
+    cpx<double> diagSum = mk(0.0, 0.0), acc = mk(0.0, 0.0);
+    for (int c0 = 0; c0 < op.num_ops; c0 += 32) {
+      const int o = c0 + lane;
+      bool valid = false;
+      int nf = 0;
+      cpx<double> m = mk(0.0, 0.0);
+      if (o < op.num_ops) {
+        bf_string_result r;
+        bf_apply_string(op, o, cfg, occ, g.sites, r);
+        if ((isdiag[o >> 5] >> (o & 31)) & 1u) {
+          diagSum = diagSum + r.m;
+        } else if (sqrt(abs2(r.m)) > 1e-6) {  // _find_nonzero threshold (base.py:96)
+          valid = true;
+          m = r.m;
+          for (int q = 0; q < r.nmod; ++q)
+            if (r.val[q] != cfg[r.site[q]]) fsRow[lane * VMC_BF_MAX_LEN + nf++] = (int16_t)r.site[q];
+        }
+      }
+      __syncwarp();
+      unsigned vmask = __ballot_sync(0xffffffffu, valid);
+      const int myNf = nf;
+      double myRatio = 1.0;
+      while (vmask) {
+        const int k = __ffs(vmask) - 1;
+        vmask &= vmask - 1;
+        const int nfk = __shfl_sync(0xffffffffu, myNf, k);
+        if (nfk == 0) continue;
+        const int16_t* fs = fsRow + k * VMC_BF_MAX_LEN;
+        T delta;
+        if (nfk == 1) {
+          delta = warp_local_delta(g, lc, prm, cfg, a, scr, fs[0], lane);
+        } else {
+          delta = T(0);
+          for (int q = 0; q < nfk; ++q) {
+            delta += warp_local_delta(g, lc, prm, cfg, a, scr, fs[q], lane);
+            warp_local_commit(g, lc, cfg, a, scr, fs[q], lane);
+          }
+          for (int q = nfk - 1; q >= 0; --q) {
+            warp_local_delta(g, lc, prm, cfg, a, scr, fs[q], lane);
+            warp_local_commit(g, lc, cfg, a, scr, fs[q], lane);
+          }
+        }
+        if (lane == k) myRatio = exp((double)delta);
+      }
+      if (valid) acc = acc + mk(m.re * myRatio, m.im * myRatio);
+      __syncwarp();
+    }
+    acc = warp_sum(acc);
+    diagSum = warp_sum(diagSum);
+    if (op.num_diag > 0 && sqrt(abs2(diagSum)) > 1e-6) acc = acc + diagSum;
+    if (logPsiS) {
+      const double2 gv = logPsiS[n];
+      acc = acc * cexp_(mk((double)lpNet - gv.x, -gv.y));
+    }
+    if (lane == 0) out[n] = make_double2(acc.re, acc.im);
+    __syncwarp();
+  }
 }
 
 }  // namespace vmc
@@ -429,23 +726,68 @@ extern "C" int vmc_cnn_metropolis(int32_t precision, const vmc_cnn_desc* desc, i
   VMC_REQUIRE(therm_steps + sweep_steps * samples_per_chain < (int64_t)0xFFFFFFFF, VMC_ERR_UNSUPPORTED,
               "vmc_cnn_metropolis: more than 2^32 steps in one call");
   const size_t el = precision == VMC_F64 ? 8 : 4;
-  const size_t per = ((size_t)g.layers * g.sites * g.maxC * el + 2 * g.sites + 15) & ~(size_t)15;
-  int warps = pick_warps(per, 4, "vmc_cnn_metropolis");
-  if (!warps) return VMC_ERR_UNSUPPORTED;
-  const size_t smem = per * warps;
+  const cnn_local lc = make_local(g);
+  const size_t per = ((size_t)lc.perWarp * el + g.sites + 15) & ~(size_t)15;
+  const size_t prmBytes = ((size_t)g.P * el + 15) & ~(size_t)15;
+  const bool inSmem = prmBytes <= (size_t)kCnnParamSmem;
+  int warps = 4;
+  while (warps > 1 && (inSmem ? prmBytes : 0) + per * warps > 200 * 1024) warps /= 2;
+  const size_t smem = (inSmem ? prmBytes : 0) + per * warps;
+  VMC_REQUIRE(smem <= 227 * 1024, VMC_ERR_UNSUPPORTED, "vmc_cnn_metropolis: network too large for shared memory");
   const int grid = (num_chains + warps - 1) / warps;
   cudaStream_t st = as_stream(stream);
   unsigned long long* cnt = reinterpret_cast<unsigned long long*>(counters);
   if (precision == VMC_F64) {
-    allow_smem(cnn_metropolis_kernel<double>, smem);
-    cnn_metropolis_kernel<double><<<grid, 32 * warps, smem, st>>>(
-        states, num_chains, g, reinterpret_cast<const double*>(params), warps, mu, seed, call_index, therm_steps,
-        sweep_steps, samples_per_chain, configs_out, cnt);
+    allow_smem(cnn_metropolis_local_kernel<double>, smem);
+    cnn_metropolis_local_kernel<double><<<grid, 32 * warps, smem, st>>>(
+        states, num_chains, g, lc, reinterpret_cast<const double*>(params), warps, inSmem, mu, seed, call_index,
+        therm_steps, sweep_steps, samples_per_chain, configs_out, cnt);
   } else {
-    allow_smem(cnn_metropolis_kernel<float>, smem);
-    cnn_metropolis_kernel<float><<<grid, 32 * warps, smem, st>>>(
-        states, num_chains, g, reinterpret_cast<const float*>(params), warps, mu, seed, call_index, therm_steps,
-        sweep_steps, samples_per_chain, configs_out, cnt);
+    allow_smem(cnn_metropolis_local_kernel<float>, smem);
+    cnn_metropolis_local_kernel<float><<<grid, 32 * warps, smem, st>>>(
+        states, num_chains, g, lc, reinterpret_cast<const float*>(params), warps, inSmem, mu, seed, call_index,
+        therm_steps, sweep_steps, samples_per_chain, configs_out, cnt);
   }
   return check_launch("vmc_cnn_metropolis");
+}
+
+extern "C" int vmc_cnn_oloc_fused(int32_t precision, const vmc_cnn_desc* desc, const int32_t* configs,
+                                  int64_t num_configs, const void* params, const vmc_bf_operator* op,
+                                  const double* log_psi_s, double* oloc, vmc_stream_t stream) {
+  cnn_geom g;
+  int rc = make_geom(desc, g);
+  if (rc) return rc;
+  VMC_REQUIRE(precision == VMC_F64 || precision == VMC_F32, VMC_ERR_UNSUPPORTED, "vmc_cnn_oloc_fused: precision");
+  if ((rc = check_op("vmc_cnn_oloc_fused", op, g.sites))) return rc;
+  VMC_REQUIRE(op->local_dim == 2, VMC_ERR_UNSUPPORTED, "vmc_cnn_oloc_fused: local dimension %d (spins need 2)",
+              op->local_dim);
+  if (num_configs == 0) return VMC_OK;
+  VMC_REQUIRE(configs && params && oloc && num_configs > 0, VMC_ERR_INVALID_ARGUMENT, "vmc_cnn_oloc_fused: null");
+  const size_t el = precision == VMC_F64 ? 8 : 4;
+  const cnn_local lc = make_local(g);
+  const int nw = (g.sites + 31) >> 5;
+  const size_t per = ((size_t)lc.perWarp * el + (size_t)nw * 4 + g.sites + 32 * VMC_BF_MAX_LEN * 2 + 15) &
+                     ~(size_t)15;
+  const size_t prmBytes = ((size_t)g.P * el + 15) & ~(size_t)15;
+  const bool inSmem = prmBytes <= (size_t)kCnnParamSmem;
+  const size_t diagBytes = ((size_t)((op->num_ops + 31) >> 5) * 4 + 15) & ~(size_t)15;
+  int warps = 4;
+  while (warps > 1 && (inSmem ? prmBytes : 0) + diagBytes + per * warps > 200 * 1024) warps /= 2;
+  const size_t smem = (inSmem ? prmBytes : 0) + diagBytes + per * warps;
+  VMC_REQUIRE(smem <= 227 * 1024, VMC_ERR_UNSUPPORTED, "vmc_cnn_oloc_fused: network too large for shared memory");
+  int64_t grid = (num_configs + warps - 1) / warps;
+  if (grid > 152 * 32) grid = 152 * 32;
+  cudaStream_t st = as_stream(stream);
+  if (precision == VMC_F64) {
+    allow_smem(cnn_oloc_fused_kernel<double>, smem);
+    cnn_oloc_fused_kernel<double><<<(int)grid, 32 * warps, smem, st>>>(
+        configs, num_configs, g, lc, reinterpret_cast<const double*>(params), warps, inSmem, *op,
+        reinterpret_cast<const double2*>(log_psi_s), reinterpret_cast<double2*>(oloc));
+  } else {
+    allow_smem(cnn_oloc_fused_kernel<float>, smem);
+    cnn_oloc_fused_kernel<float><<<(int)grid, 32 * warps, smem, st>>>(
+        configs, num_configs, g, lc, reinterpret_cast<const float*>(params), warps, inSmem, *op,
+        reinterpret_cast<const double2*>(log_psi_s), reinterpret_cast<double2*>(oloc));
+  }
+  return check_launch("vmc_cnn_oloc_fused");
 }

@@ -76,6 +76,7 @@ struct dense_args {
   const double2* eloc;      // null: gradient data
   const double2* elocMean;
   double2 xfac;             // -x
+  int realPart;             // SNR data of a real-parameter net (makeReal = Re)
   const double2* force;
   int format;
   int64_t ld;
@@ -90,7 +91,7 @@ __device__ __forceinline__ cpx<double> dense_value(const dense_args& a, int64_t 
     const double2 e = a.eloc[n], em = *a.elocMean;
     const cpx<double> h = mk(a.xfac.x, a.xfac.y) * (mk(e.x - em.x, e.y - em.y) * conjg(d));
     const double2 f = a.force[k];
-    d = mk(h.re - f.x, h.im - f.y);
+    d = a.realPart ? mk(h.re - f.x, 0.0) : mk(h.re - f.x, h.im - f.y);
   }
   const double sw = sqrt(a.w[n]);
   return mk(sw * d.re, sw * d.im);
@@ -212,6 +213,7 @@ extern "C" int vmc_dense_centered_gradients(const double* gradients, int64_t ld_
   a.eloc = nullptr;
   a.elocMean = nullptr;
   a.xfac = make_double2(0, 0);
+  a.realPart = 0;
   a.force = nullptr;
   a.format = format;
   a.ld = ld_out;
@@ -223,7 +225,8 @@ extern "C" int vmc_dense_centered_gradients(const double* gradients, int64_t ld_
 extern "C" int vmc_dense_snr_data(const double* gradients, int64_t ld_gradients, int64_t num_configs,
                                   int64_t num_params, const double* weights, const double* ok_mean, const double* eloc,
                                   const double* eloc_mean, double neg_rhs_re, double neg_rhs_im, const double* force,
-                                  int32_t format, void* out, void* out_lo, int64_t ld_out, vmc_stream_t stream) {
+                                  int32_t real_part, int32_t format, void* out, void* out_lo, int64_t ld_out,
+                                  vmc_stream_t stream) {
   VMC_REQUIRE(eloc && eloc_mean && force, VMC_ERR_INVALID_ARGUMENT, "vmc_dense_snr_data: null argument");
   dense_args a;
   a.O = reinterpret_cast<const double2*>(gradients);
@@ -235,6 +238,7 @@ extern "C" int vmc_dense_snr_data(const double* gradients, int64_t ld_gradients,
   a.eloc = reinterpret_cast<const double2*>(eloc);
   a.elocMean = reinterpret_cast<const double2*>(eloc_mean);
   a.xfac = make_double2(neg_rhs_re, neg_rhs_im);
+  a.realPart = real_part ? 1 : 0;
   a.force = reinterpret_cast<const double2*>(force);
   a.format = format;
   a.ld = ld_out;

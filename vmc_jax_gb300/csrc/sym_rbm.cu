@@ -85,36 +85,44 @@ __device__ __forceinline__ cpx<T> theta_of(const rbm_params<T>& p, const int8_t*
 // one warp; every lane returns the result).  Exp: jax's logsumexp with
 // b = factor for complex input: elements with factor 0 are dropped, the
 // largest real part m is taken out, result = m + principal log(sum).
-__device__ __forceinline__ cpx<double> sym_average(const sym_params& sp, const cpx<double>* lp, int lane) {
+// U: the arithmetic (double, or float inside the FP32 sampler).
+__device__ __forceinline__ float warp_max(float v) {
+#pragma unroll
+  for (int m = 16; m >= 1; m >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, m));
+  return v;
+}
+
+template <typename U>
+__device__ __forceinline__ cpx<U> sym_average(const sym_params& sp, const cpx<U>* lp, int lane) {
   if (sp.avg == VMC_SYM_LOG) {
-    cpx<double> s = mk(0.0, 0.0);
+    cpx<U> s = mk(U(0), U(0));
     for (int t = lane; t < sp.S; t += 32) s = s + lp[t];
     s = warp_sum(s);
-    return mk(s.re / sp.S, s.im / sp.S);
+    return mk(s.re / U(sp.S), s.im / U(sp.S));
   }
-  double mx = -INFINITY;
+  U mx = -INFINITY;
   for (int t = lane; t < sp.S; t += 32) {
     const double2 f = sp.factor[t];
     if (f.x != 0.0 || f.y != 0.0) mx = fmax(mx, lp[t].re);
   }
   mx = warp_max(mx);
-  if (!isfinite(mx)) mx = 0.0;
-  cpx<double> z = mk(0.0, 0.0);
+  if (!isfinite(mx)) mx = U(0);
+  cpx<U> z = mk(U(0), U(0));
   for (int t = lane; t < sp.S; t += 32) {
     const double2 f = sp.factor[t];
-    if (f.x != 0.0 || f.y != 0.0) z = z + mk(f.x, f.y) * cexp_(mk(lp[t].re - mx, lp[t].im));
+    if (f.x != 0.0 || f.y != 0.0) z = z + mk((U)f.x, (U)f.y) * cexp_(mk(lp[t].re - mx, lp[t].im));
   }
   z = warp_sum(z);
-  return mk(mx + log(hypot(z.re, z.im)), atan2(z.im, z.re));
+  return mk(mx + flog(fhypot(z.re, z.im)), fatan2(z.im, z.re));
 }
 
 // weight of element t in d log psi: f_t exp(lp_t - log psi) (Exp) or 1/S (Log)
-__device__ __forceinline__ cpx<double> sym_weight(const sym_params& sp, const cpx<double>* lp, cpx<double> lsym,
-                                                  int t) {
-  if (sp.avg == VMC_SYM_LOG) return mk(1.0 / sp.S, 0.0);
+template <typename U>
+__device__ __forceinline__ cpx<U> sym_weight(const sym_params& sp, const cpx<U>* lp, cpx<U> lsym, int t) {
+  if (sp.avg == VMC_SYM_LOG) return mk(U(1) / U(sp.S), U(0));
   const double2 f = sp.factor[t];
-  if (f.x == 0.0 && f.y == 0.0) return mk(0.0, 0.0);
-  return mk(f.x, f.y) * cexp_(mk(lp[t].re - lsym.re, lp[t].im - lsym.im));
+  if (f.x == 0.0 && f.y == 0.0) return mk(U(0), U(0));
+  return mk((U)f.x, (U)f.y) * cexp_(mk(lp[t].re - lsym.re, lp[t].im - lsym.im));
 }
 
 // log psi of every orbit element of cfg into lp (all warps; ends synchronised)
@@ -255,28 +263,30 @@ __global__ void __launch_bounds__(kSymThreads) sym_rbm_grad_kernel(const int32_t
 // the plain kernel's one-flip / several-flip factors, at the positions of
 // tau(s) that the string's flipped sites map to.  Per pass every thread
 // applies one string; the nonzero flipping strings are compacted in string
-// order (ballots, so the summation order is fixed); each warp then forms
-// sum_k m_k r_tau,k for its orbit elements.
-template <typename T>
+// order (ballots, so the summation order is fixed).  Then G threads per
+// orbit element (JPT hidden units each, tanh(theta) in registers) form
+// sum_k m_k r_tau,k, the product over the G threads by a butterfly.
+template <typename T, int JPT>
 __global__ void __launch_bounds__(kSymThreads) sym_rbm_oloc_fused_kernel(
     const int32_t* __restrict__ configs, int64_t N, rbm_params<T> p, sym_params sp, const cpx<T>* __restrict__ tab,
-    vmc_bf_operator op, const double2* __restrict__ logPsiS, double2* __restrict__ out) {
+    vmc_bf_operator op, int G, const double2* __restrict__ logPsiS, double2* __restrict__ out) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int gid = threadIdx.x / G, sub = threadIdx.x - gid * G, nGroups = kSymThreads / G;
   const int L = p.L, M = p.M, Lp = (L + 15) & ~15;
   const int nw = (L + 31) >> 5;
   const int diagWords = (op.num_ops + 31) >> 5;
   cpx<double>* lp = reinterpret_cast<cpx<double>*>(smem);
   cpx<double>* A = lp + sp.S;
   cpx<double>* cm = A + sp.S;
-  cpx<T>* th = reinterpret_cast<cpx<T>*>(cm + kSymChunk) + (size_t)warp * M;
-  uint32_t* isdiag = reinterpret_cast<uint32_t*>(reinterpret_cast<cpx<T>*>(cm + kSymChunk) + (size_t)kSymWarps * M);
+  uint32_t* isdiag = reinterpret_cast<uint32_t*>(cm + kSymChunk);
   uint32_t* occ = isdiag + diagWords;
   int* wcount = reinterpret_cast<int*>(occ + nw);
   int16_t* cfs = reinterpret_cast<int16_t*>(wcount + kSymWarps);
   int8_t* cnf = reinterpret_cast<int8_t*>(cfs + (size_t)kSymChunk * VMC_BF_MAX_LEN);
-  int8_t* cfg = cnf + kSymChunk;
-  int8_t* tcfg = cfg + Lp + warp * Lp;
+  int8_t* bad = cnf + kSymChunk;        // per orbit element: malformed orbit tables
+  int8_t* cfg = bad + ((sp.S + 15) & ~15);
+  int8_t* tcfg = cfg + Lp;              // (S, Lp): tau(s) of every orbit element
 
   for (int w = threadIdx.x; w < diagWords; w += blockDim.x) isdiag[w] = 0u;
   __syncthreads();
@@ -294,7 +304,15 @@ __global__ void __launch_bounds__(kSymThreads) sym_rbm_oloc_fused_kernel(
 
   for (int64_t n = blockIdx.x; n < N; n += gridDim.x) {
     if (warp == 0) warp_load_config(configs + n * L, L, cfg, occ, lane);
-    for (int t = threadIdx.x; t < sp.S; t += blockDim.x) A[t] = mk(0.0, 0.0);
+    for (int t = threadIdx.x; t < sp.S; t += blockDim.x) {
+      A[t] = mk(0.0, 0.0);
+      bad[t] = 0;
+    }
+    __syncthreads();
+    for (int t = warp; t < sp.S; t += kSymWarps) {
+      const bool ok = sym_transform(sp.code + (size_t)t * L, cfg, L, tcfg + (size_t)t * Lp, lane);
+      if (lane == 0 && !ok) bad[t] = 1;
+    }
     __syncthreads();
     cpx<double> diagAcc = mk(0.0, 0.0), constAcc = mk(0.0, 0.0);
     // at least one pass: it also forms the per-element log psi
@@ -335,19 +353,29 @@ __global__ void __launch_bounds__(kSymThreads) sym_rbm_oloc_fused_kernel(
         for (int q = 0; q < nf; ++q) cfs[pos * VMC_BF_MAX_LEN + q] = fsl[q];
       }
       __syncthreads();
-      for (int t = warp; t < sp.S; t += kSymWarps) {
-        const int32_t* inv = sp.inv + (size_t)t * L;
-        bool ok = sym_transform(sp.code + (size_t)t * L, cfg, L, tcfg, lane);
+      // same trip counts on every thread: the group butterflies see full warps
+      for (int t0 = 0; t0 < sp.S; t0 += nGroups) {
+        const int t = t0 + gid;
+        const bool active = t < sp.S;
+        const int tt = active ? t : 0;
+        const int8_t* tc = tcfg + (size_t)tt * Lp;
+        const int32_t* inv = sp.inv + (size_t)tt * L;
+        cpx<T> th[JPT];
         cpx<T> lpt = mk(T(0), T(0));
-        for (int j = lane; j < M; j += 32) {
-          const cpx<T> x = theta_of(p, tcfg, j);
-          if (c0 == 0) lpt = lpt + log_cosh(x);
-          th[j] = ctanh_(x);
+#pragma unroll
+        for (int q = 0; q < JPT; ++q) {
+          const int j = sub + q * G;
+          if (active && j < M) {
+            const cpx<T> x = theta_of(p, tc, j);
+            if (c0 == 0) lpt = lpt + log_cosh(x);
+            th[q] = ctanh_(x);
+          } else {
+            th[q] = mk(T(0), T(0));
+          }
         }
-        __syncwarp();
         if (c0 == 0) {
-          lpt = warp_sum(lpt);
-          if (lane == 0) lp[t] = mk((double)lpt.re, (double)lpt.im);
+          for (int mm = 1; mm < G; mm <<= 1) lpt = lpt + shfl_xor(lpt, mm);
+          if (active && sub == 0) lp[t] = mk((double)lpt.re, (double)lpt.im);
         }
         cpx<double> acc = mk(0.0, 0.0);
         for (int k = 0; k < total; ++k) {
@@ -356,68 +384,66 @@ __global__ void __launch_bounds__(kSymThreads) sym_rbm_oloc_fused_kernel(
           scaled_cpx<T> prod;
           prod.m = mk(T(1), T(0));
           prod.ex = 0;
-          int cnt = 0;
-          if (nfk == 1) {
+          bool good = active;
+          for (int q = 0; q < nfk; ++q) good = good && (unsigned)inv[fs[q]] < (unsigned)L;
+          if (!active) {
+          } else if (!good) {
+            prod.m = mk(T(nan("")), T(nan("")));
+          } else if (nfk == 1) {
             const int pi = inv[fs[0]];
-            if ((unsigned)pi >= (unsigned)L) {
-              ok = false;
-              continue;
-            }
-            const T sg = tcfg[pi] ? T(1) : T(-1);
+            const T sg = tc[pi] ? T(1) : T(-1);
             const cpx<T>* rc = tC + (size_t)pi * M;
             const cpx<T>* rs = tS + (size_t)pi * M;
-            for (int j = lane; j < M; j += 32) {
-              prod.m = prod.m * (rc[j] - sg * (th[j] * rs[j]));
-              if (++cnt == 8) {
-                renorm(prod);
-                cnt = 0;
-              }
+#pragma unroll
+            for (int q = 0; q < JPT; ++q) {
+              const int j = sub + q * G;
+              if (j < M) prod.m = prod.m * (rc[j] - sg * (th[q] * rs[j]));
+              if ((q & 7) == 7) renorm(prod);
             }
           } else {
-            bool good = true;
-            for (int q = 0; q < nfk; ++q) good = good && (unsigned)inv[fs[q]] < (unsigned)L;
-            if (!good) {
-              ok = false;
-              continue;
-            }
-            for (int j = lane; j < M; j += 32) {
-              cpx<T> e1 = mk(T(1), T(0)), e2 = mk(T(1), T(0));
-              for (int q = 0; q < nfk; ++q) {
-                const int pq = inv[fs[q]];
-                const cpx<T> ea = tEp[(size_t)pq * M + j], eb = tEm[(size_t)pq * M + j];
-                if (tcfg[pq]) {
-                  e1 = e1 * eb;
-                  e2 = e2 * ea;
-                } else {
-                  e1 = e1 * ea;
-                  e2 = e2 * eb;
+#pragma unroll
+            for (int q = 0; q < JPT; ++q) {
+              const int j = sub + q * G;
+              if (j < M) {
+                cpx<T> e1 = mk(T(1), T(0)), e2 = mk(T(1), T(0));
+                for (int qq = 0; qq < nfk; ++qq) {
+                  const int pq = inv[fs[qq]];
+                  const cpx<T> ea = tEp[(size_t)pq * M + j], eb = tEm[(size_t)pq * M + j];
+                  if (tc[pq]) {
+                    e1 = e1 * eb;
+                    e2 = e2 * ea;
+                  } else {
+                    e1 = e1 * ea;
+                    e2 = e2 * eb;
+                  }
                 }
+                const cpx<T> tj = th[q];
+                const cpx<T> onep = mk(T(1) + tj.re, tj.im), onem = mk(T(1) - tj.re, -tj.im);
+                prod.m = prod.m * (T(0.5) * (onep * e1 + onem * e2));
               }
-              const cpx<T> tj = th[j];
-              const cpx<T> onep = mk(T(1) + tj.re, tj.im), onem = mk(T(1) - tj.re, -tj.im);
-              prod.m = prod.m * (T(0.5) * (onep * e1 + onem * e2));
-              if (++cnt == 8) {
-                renorm(prod);
-                cnt = 0;
-              }
+              if ((q & 7) == 7) renorm(prod);
             }
           }
           renorm(prod);
-          prod = warp_prod(prod);
+          for (int mm = 1; mm < G; mm <<= 1) {
+            scaled_cpx<T> o2;
+            o2.m = shfl_xor(prod.m, mm);
+            o2.ex = __shfl_xor_sync(0xffffffffu, prod.ex, mm);
+            prod = mul(prod, o2);
+          }
           const cpx<T> r = to_cpx(prod);
           acc = acc + cm[k] * mk((double)r.re, (double)r.im);
         }
-        if (lane == 0) {
-          A[t] = ok ? A[t] + acc : mk(nan(""), nan(""));
-          if (!ok) lp[t] = mk(nan(""), nan(""));
-        }
-        __syncwarp();
+        if (active && sub == 0) A[t] = A[t] + acc;
       }
       __syncthreads();
     }
     const double dr = block_sum(diagAcc.re), di = block_sum(diagAcc.im);
     const double cr = block_sum(constAcc.re), ci = block_sum(constAcc.im);
     if (warp == 0) {
+      for (int t = lane; t < sp.S; t += 32)
+        if (bad[t]) lp[t] = mk(nan(""), nan(""));
+      __syncwarp();
       const cpx<double> lsym = sym_average(sp, lp, lane);
       cpx<double> E = mk(0.0, 0.0);
       for (int t = lane; t < sp.S; t += 32) E = E + sym_weight(sp, lp, lsym, t) * A[t];
@@ -447,7 +473,7 @@ __global__ void __launch_bounds__(kSymThreads) sym_rbm_oloc_fused_kernel(
 // from the configuration, so rounding does not accumulate.
 template <typename T>
 __device__ void sym_mc_rebuild(const rbm_params<T>& p, const sym_params& sp, const int8_t* cfg, int8_t* tcfg,
-                               cpx<T>* tst, cpx<double>* w, int warp, int lane) {
+                               cpx<T>* tst, cpx<T>* w, int warp, int lane) {
   for (int t = warp; t < sp.S; t += kSymWarps) {
     const bool ok = sym_transform(sp.code + (size_t)t * p.L, cfg, p.L, tcfg, lane);
     cpx<T> acc = mk(T(0), T(0));
@@ -457,12 +483,12 @@ __device__ void sym_mc_rebuild(const rbm_params<T>& p, const sym_params& sp, con
       tst[(size_t)t * p.M + j] = ctanh_(x);
     }
     acc = warp_sum(acc);
-    if (lane == 0) w[t] = ok ? mk((double)acc.re, (double)acc.im) : mk(nan(""), nan(""));
+    if (lane == 0) w[t] = ok ? acc : mk(T(nan("")), T(nan("")));
     __syncwarp();
   }
   __syncthreads();
   if (warp == 0 && sp.avg == VMC_SYM_EXP) {
-    const cpx<double> lsym = sym_average(sp, w, lane);  // every lane holds it before w is overwritten
+    const cpx<T> lsym = sym_average(sp, w, lane);  // every lane holds it before w is overwritten
     for (int t = lane; t < sp.S; t += 32) w[t] = sym_weight(sp, w, lsym, t);
   }
   __syncthreads();
@@ -471,17 +497,20 @@ __device__ void sym_mc_rebuild(const rbm_params<T>& p, const sym_params& sp, con
 template <typename T>
 __global__ void __launch_bounds__(kSymThreads) sym_rbm_metropolis_kernel(
     int32_t* __restrict__ states, int C, rbm_params<T> p, sym_params sp, const cpx<T>* __restrict__ tab, double mu,
-    uint64_t seed, uint32_t call, int64_t thermSteps, int64_t sweepSteps, int64_t samplesPerChain,
+    uint64_t seed, uint32_t call, int64_t thermSteps, int64_t sweepSteps, int64_t samplesPerChain, int G,
     int32_t* __restrict__ configsOut, unsigned long long* __restrict__ counters) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ int sAcc;
-  __shared__ cpx<double> sR;
+  __shared__ cpx<T> sR;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int gid = threadIdx.x / G, sub = threadIdx.x - gid * G, nGroups = kSymThreads / G;
   const int chain = blockIdx.x;
   const int L = p.L, M = p.M, Lp = (L + 15) & ~15;
-  cpx<double>* w = reinterpret_cast<cpx<double>*>(smem);
-  cpx<double>* rat = w + sp.S;
-  cpx<T>* tst = reinterpret_cast<cpx<T>*>(rat + sp.S);
+  // weights, ratios and the decision in the kernel's arithmetic T (the FP32
+  // sampler does no FP64 work per proposal)
+  cpx<T>* w = reinterpret_cast<cpx<T>*>(smem);
+  cpx<T>* rat = w + sp.S;
+  cpx<T>* tst = rat + sp.S;
   int8_t* cfg = reinterpret_cast<int8_t*>(tst + (size_t)sp.S * M);
   int8_t* tcfg = cfg + Lp + warp * Lp;
   int32_t* st = states + (size_t)chain * L;
@@ -497,19 +526,25 @@ __global__ void __launch_bounds__(kSymThreads) sym_rbm_metropolis_kernel(
   for (int64_t step = 0; step < total; ++step) {
     const mc_draw d = metropolis_draw(seed, call, (uint32_t)step, (uint32_t)chain, L);
     const int i = d.site;
-    for (int t = warp; t < sp.S; t += kSymWarps) {
-      const int pi = sp.inv[(size_t)t * L + i];
+    // G threads per orbit element: partial products over j = sub, sub + G, ..
+    // then a butterfly over the G lanes of the group.  The trip count is the
+    // same for every thread (t0 loop), so the shuffles see full warps.
+    for (int t0 = 0; t0 < sp.S; t0 += nGroups) {
+      const int t = t0 + gid;
+      const bool active = t < sp.S;
+      const int pi = active ? sp.inv[(size_t)t * L + i] : 0;
       scaled_cpx<T> prod;
       prod.m = mk(T(1), T(0));
       prod.ex = 0;
-      if ((unsigned)pi < (unsigned)L) {
+      if (!active) {
+      } else if ((unsigned)pi < (unsigned)L) {
         const int c = sp.code[(size_t)t * L + pi];
         const T sg = (cfg[i] ^ (c & 1)) ? T(1) : T(-1);
         const cpx<T>* rc = tC + (size_t)pi * M;
         const cpx<T>* rs = tS + (size_t)pi * M;
         const cpx<T>* tt = tst + (size_t)t * M;
         int cnt = 0;
-        for (int j = lane; j < M; j += 32) {
+        for (int j = sub; j < M; j += G) {
           prod.m = prod.m * (rc[j] - sg * (tt[j] * rs[j]));
           if (++cnt == 8) {
             renorm(prod);
@@ -520,37 +555,48 @@ __global__ void __launch_bounds__(kSymThreads) sym_rbm_metropolis_kernel(
         prod.m = mk(T(nan("")), T(nan("")));
       }
       renorm(prod);
-      prod = warp_prod(prod);
-      if (lane == 0) {
-        double e = (double)prod.ex;
-        rat[t] = mk(ldexp((double)prod.m.re, (int)fmin(fmax(e, -2000.0), 2000.0)),
-                    ldexp((double)prod.m.im, (int)fmin(fmax(e, -2000.0), 2000.0)));
+      for (int m = 1; m < G; m <<= 1) {
+        scaled_cpx<T> o;
+        o.m = shfl_xor(prod.m, m);
+        o.ex = __shfl_xor_sync(0xffffffffu, prod.ex, m);
+        prod = mul(prod, o);
+      }
+      if (active && sub == 0) {
+        // ratios beyond the float range saturate (they decide acceptance alone)
+        const int lim = sizeof(T) == sizeof(double) ? 2000 : 120;
+        const int e = max(-lim, min(lim, prod.ex));
+        rat[t] = mk(ldexp(prod.m.re, e), ldexp(prod.m.im, e));
       }
     }
     __syncthreads();
     if (warp == 0) {
-      double logr2;
-      cpx<double> R = mk(0.0, 0.0);
+      T logr2;
+      cpx<T> R = mk(T(0), T(0));
       if (sp.avg == VMC_SYM_EXP) {
         for (int t = lane; t < sp.S; t += 32) R = R + w[t] * rat[t];
         R = warp_sum(R);
-        logr2 = log(abs2(R));
+        logr2 = flog(abs2(R));
       } else {
-        double s = 0.0;
-        for (int t = lane; t < sp.S; t += 32) s += log(abs2(rat[t]));
-        logr2 = warp_sum(s) / sp.S;
+        T s = T(0);
+        for (int t = lane; t < sp.S; t += 32) s += flog(abs2(rat[t]));
+        logr2 = warp_sum(s) / T(sp.S);
       }
       // P = |psi(s')/psi(s)|^mu; accept iff u < P (bernoulli, sampler.py:339-340)
-      const double P = exp(0.5 * mu * logr2);
+      bool acc;
+      if (sizeof(T) == sizeof(double)) {
+        acc = d.u64() < exp(0.5 * mu * (double)logr2);
+      } else {
+        acc = d.u32() < expf(0.5f * (float)mu * (float)logr2);
+      }
       if (lane == 0) {
-        sAcc = d.u64() < P ? 1 : 0;
+        sAcc = acc ? 1 : 0;
         sR = R;
       }
     }
     __syncthreads();
     if (sAcc) {
-      const cpx<double> R = sR;
-      for (int t = warp; t < sp.S; t += kSymWarps) {
+      const cpx<T> R = sR;
+      for (int t = gid; t < sp.S; t += nGroups) {
         const int pi = sp.inv[(size_t)t * L + i];
         if ((unsigned)pi < (unsigned)L) {
           const int c = sp.code[(size_t)t * L + pi];
@@ -558,12 +604,12 @@ __global__ void __launch_bounds__(kSymThreads) sym_rbm_metropolis_kernel(
           const cpx<T>* rc = tC + (size_t)pi * M;
           const cpx<T>* rs = tS + (size_t)pi * M;
           cpx<T>* tt = tst + (size_t)t * M;
-          for (int j = lane; j < M; j += 32) {
+          for (int j = sub; j < M; j += G) {
             const cpx<T> cj = rc[j], sj = rs[j], tj = tt[j];
             tt[j] = cdiv(tj * cj - sg * sj, cj - sg * (tj * sj));
           }
         }
-        if (lane == 0 && sp.avg == VMC_SYM_EXP) w[t] = cdiv(w[t] * rat[t], R);
+        if (sub == 0 && sp.avg == VMC_SYM_EXP) w[t] = cdiv(w[t] * rat[t], R);
       }
       __syncthreads();
       if (threadIdx.x == 0) {
@@ -606,6 +652,15 @@ sym_params make_sym(const vmc_sym_desc* s) {
   sp.inv = s->inverse;
   sp.factor = reinterpret_cast<const double2*>(s->factor);
   return sp;
+}
+
+// threads per orbit element in the per-proposal kernels: a power of two
+// <= 32 that spreads the block's threads over the orbit and keeps at least
+// a few hidden units per thread
+int group_size(int S, int M) {
+  int G = 32;
+  while (G > 1 && (G * S > kSymThreads || G * 4 > M)) G >>= 1;
+  return G;
 }
 
 int sym_grid(int64_t N) { return (int)std::max<int64_t>(1, std::min<int64_t>(N, 152 * 4)); }
@@ -679,6 +734,27 @@ extern "C" int vmc_sym_rbm_gradients(int32_t precision, const int32_t* configs, 
   return check_launch("vmc_sym_rbm_gradients");
 }
 
+template <typename T, int JPT>
+static void launch_sym_oloc(int grid, size_t smem, cudaStream_t st, const int32_t* configs, int64_t N,
+                            rbm_params<T> p, sym_params sp, const void* tables, const vmc_bf_operator* op, int G,
+                            const double* lps, double* out) {
+  set_smem((const void*)sym_rbm_oloc_fused_kernel<T, JPT>, smem);
+  sym_rbm_oloc_fused_kernel<T, JPT><<<grid, kSymThreads, smem, st>>>(
+      configs, N, p, sp, reinterpret_cast<const cpx<T>*>(tables), *op, G, reinterpret_cast<const double2*>(lps),
+      reinterpret_cast<double2*>(out));
+}
+
+template <typename T>
+static int dispatch_sym_oloc(int jpt, int grid, size_t smem, cudaStream_t st, const int32_t* configs, int64_t N,
+                             rbm_params<T> p, sym_params sp, const void* tables, const vmc_bf_operator* op, int G,
+                             const double* lps, double* out) {
+  if (jpt <= 2) launch_sym_oloc<T, 2>(grid, smem, st, configs, N, p, sp, tables, op, G, lps, out);
+  else if (jpt <= 4) launch_sym_oloc<T, 4>(grid, smem, st, configs, N, p, sp, tables, op, G, lps, out);
+  else if (jpt <= 8) launch_sym_oloc<T, 8>(grid, smem, st, configs, N, p, sp, tables, op, G, lps, out);
+  else launch_sym_oloc<T, 16>(grid, smem, st, configs, N, p, sp, tables, op, G, lps, out);
+  return check_launch("vmc_sym_rbm_oloc_fused");
+}
+
 extern "C" int vmc_sym_rbm_oloc_fused(int32_t precision, const int32_t* configs, int64_t num_configs,
                                       int32_t num_sites, int32_t num_hidden, const void* kernel, const void* bias,
                                       const void* tables, const vmc_sym_desc* sym, const vmc_bf_operator* op,
@@ -691,33 +767,32 @@ extern "C" int vmc_sym_rbm_oloc_fused(int32_t precision, const int32_t* configs,
               "vmc_sym_rbm_oloc_fused: only the Exp average has a fused estimator");
   VMC_REQUIRE(op->local_dim == 2, VMC_ERR_UNSUPPORTED, "vmc_sym_rbm_oloc_fused: local dimension %d (RBM needs 2)",
               op->local_dim);
+  VMC_REQUIRE(num_hidden <= 32 * 16, VMC_ERR_UNSUPPORTED, "vmc_sym_rbm_oloc_fused: M=%d > 512", num_hidden);
   VMC_REQUIRE(tables && (oloc || num_configs == 0), VMC_ERR_INVALID_ARGUMENT,
               "vmc_sym_rbm_oloc_fused: null argument");
   if (num_configs == 0) return VMC_OK;
+  // threads per orbit element: at most 8 hidden units per thread (16 when
+  // M > 256), which keeps tanh(theta) in registers at two blocks per SM
+  int G = group_size(sym->num_sym, num_hidden);
+  while (G < 32 && (num_hidden + G - 1) / G > 8) G <<= 1;
+  const int jpt = (num_hidden + G - 1) / G;
   const int Lp = (num_sites + 15) & ~15;
-  const size_t el = precision == VMC_F64 ? 16 : 8;
   const int nw = (num_sites + 31) >> 5;
   const int diagWords = (op->num_ops + 31) >> 5;
-  const size_t smem = 2 * lp_bytes(sym->num_sym) + (size_t)kSymChunk * 16 + (size_t)kSymWarps * num_hidden * el +
+  const size_t smem = 2 * lp_bytes(sym->num_sym) + (size_t)kSymChunk * 16 +
                       (size_t)(diagWords + nw + kSymWarps) * 4 + (size_t)kSymChunk * VMC_BF_MAX_LEN * 2 + kSymChunk +
-                      (size_t)(1 + kSymWarps) * Lp;
+                      (size_t)((sym->num_sym + 15) & ~15) + Lp + (size_t)sym->num_sym * Lp;
   VMC_REQUIRE(smem <= kSmemLimit, VMC_ERR_UNSUPPORTED, "vmc_sym_rbm_oloc_fused: problem too large");
   cudaStream_t st = as_stream(stream);
   const sym_params sp = make_sym(sym);
-  if (precision == VMC_F64) {
-    set_smem((const void*)sym_rbm_oloc_fused_kernel<double>, smem);
-    sym_rbm_oloc_fused_kernel<double><<<sym_grid(num_configs), kSymThreads, smem, st>>>(
-        configs, num_configs, make_params<double>(kernel, bias, num_sites, num_hidden), sp,
-        reinterpret_cast<const cpx<double>*>(tables), *op, reinterpret_cast<const double2*>(log_psi_s),
-        reinterpret_cast<double2*>(oloc));
-  } else {
-    set_smem((const void*)sym_rbm_oloc_fused_kernel<float>, smem);
-    sym_rbm_oloc_fused_kernel<float><<<sym_grid(num_configs), kSymThreads, smem, st>>>(
-        configs, num_configs, make_params<float>(kernel, bias, num_sites, num_hidden), sp,
-        reinterpret_cast<const cpx<float>*>(tables), *op, reinterpret_cast<const double2*>(log_psi_s),
-        reinterpret_cast<double2*>(oloc));
-  }
-  return check_launch("vmc_sym_rbm_oloc_fused");
+  const int grid = sym_grid(num_configs);
+  if (precision == VMC_F64)
+    return dispatch_sym_oloc<double>(jpt, grid, smem, st, configs, num_configs,
+                                     make_params<double>(kernel, bias, num_sites, num_hidden), sp, tables, op, G,
+                                     log_psi_s, oloc);
+  return dispatch_sym_oloc<float>(jpt, grid, smem, st, configs, num_configs,
+                                  make_params<float>(kernel, bias, num_sites, num_hidden), sp, tables, op, G, log_psi_s,
+                                  oloc);
 }
 
 extern "C" int vmc_sym_rbm_metropolis(int32_t precision, int32_t* states, int32_t num_chains, int32_t num_sites,
@@ -736,24 +811,25 @@ extern "C" int vmc_sym_rbm_metropolis(int32_t precision, int32_t* states, int32_
   VMC_REQUIRE(mu >= 0.0 && mu <= 2.0, VMC_ERR_INVALID_ARGUMENT, "vmc_sym_rbm_metropolis: mu=%g outside [0, 2]", mu);
   const int Lp = (num_sites + 15) & ~15;
   const size_t el = precision == VMC_F64 ? 16 : 8;
-  const size_t smem = 2 * lp_bytes(sym->num_sym) + (size_t)sym->num_sym * num_hidden * el + (size_t)(1 + kSymWarps) * Lp;
+  const size_t smem = (2 + (size_t)num_hidden) * sym->num_sym * el + (size_t)(1 + kSymWarps) * Lp;
   VMC_REQUIRE(smem <= kSmemLimit, VMC_ERR_UNSUPPORTED,
               "vmc_sym_rbm_metropolis: %d orbit elements x %d hidden units do not fit in shared memory", sym->num_sym,
               num_hidden);
   cudaStream_t st = as_stream(stream);
   const sym_params sp = make_sym(sym);
+  const int G = group_size(sym->num_sym, num_hidden);
   if (precision == VMC_F64) {
     set_smem((const void*)sym_rbm_metropolis_kernel<double>, smem);
     sym_rbm_metropolis_kernel<double><<<num_chains, kSymThreads, smem, st>>>(
         states, num_chains, make_params<double>(kernel, bias, num_sites, num_hidden), sp,
         reinterpret_cast<const cpx<double>*>(tables), mu, seed, call_index, therm_steps, sweep_steps, samples_per_chain,
-        configs_out, reinterpret_cast<unsigned long long*>(counters));
+        G, configs_out, reinterpret_cast<unsigned long long*>(counters));
   } else {
     set_smem((const void*)sym_rbm_metropolis_kernel<float>, smem);
     sym_rbm_metropolis_kernel<float><<<num_chains, kSymThreads, smem, st>>>(
         states, num_chains, make_params<float>(kernel, bias, num_sites, num_hidden), sp,
         reinterpret_cast<const cpx<float>*>(tables), mu, seed, call_index, therm_steps, sweep_steps, samples_per_chain,
-        configs_out, reinterpret_cast<unsigned long long*>(counters));
+        G, configs_out, reinterpret_cast<unsigned long long*>(counters));
   }
   return check_launch("vmc_sym_rbm_metropolis");
 }

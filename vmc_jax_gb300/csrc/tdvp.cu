@@ -13,9 +13,11 @@ namespace vmc {
 // matrix G = R^T R of the real representation R = [Re X | Im X], reading only
 // entries with row <= col (upper tiles), with A[b][a] = conj(A[a][b]) and
 // the diagonal shift A[a][a] *= 1 + shift (tdvp.py:144-145).
-// 32 x 32 output tiles (a0 <= b0 tile pairs): the four G blocks a tile needs
-// are read row-wise (coalesced), the transposed one through shared memory,
-// and A[a][b], A[b][a] = conj(A[a][b]) are both written row-wise.
+// 32 x 32 output tiles (a0 <= b0 tile pairs): the G blocks a tile needs are
+// read row-wise (coalesced), the transposed one through shared memory, and
+// A[a][b] (a <= b), A[b][a] = conj(A[a][b]) are both written row-wise.  In a
+// diagonal tile only a <= b is formed from G (the Gram kernel leaves some
+// entries below the diagonal unwritten) and mirrored.
 template <typename T>
 __global__ void gram_to_hermitian_kernel(const T* __restrict__ G, int64_t ldg, int P, double shift,
                                          double2* __restrict__ A) {
@@ -37,7 +39,7 @@ __global__ void gram_to_hermitian_kernel(const T* __restrict__ G, int64_t ldg, i
     for (int r = ty; r < 32; r += 8) {
       const int a = a0 + r, b = b0 + tx;
       double re = 0.0, im = 0.0;
-      if (a < P && b < P) {
+      if (a < P && b < P && (ti != tj || a <= b)) {
         // row a, columns b: G[a][b], G[P+a][P+b], G[a][P+b] (all contiguous in b)
         re = (double)G[(int64_t)a * ldg + b] + (double)G[(int64_t)(P + a) * ldg + P + b];
         im = (double)G[(int64_t)a * ldg + P + b] - sT[tx][r];
@@ -51,12 +53,10 @@ __global__ void gram_to_hermitian_kernel(const T* __restrict__ G, int64_t ldg, i
       sIm[r][tx] = im;
     }
     __syncthreads();
-    if (ti != tj) {
-      // lower tile: A[b][a] = conj(A[a][b]), written row-wise in a
-      for (int r = ty; r < 32; r += 8) {
-        const int b = b0 + r, a = a0 + tx;
-        if (a < P && b < P) A[(int64_t)b * P + a] = make_double2(sRe[tx][r], -sIm[tx][r]);
-      }
+    // mirrored entries: A[b][a] = conj(A[a][b]), written row-wise in a
+    for (int r = ty; r < 32; r += 8) {
+      const int b = b0 + r, a = a0 + tx;
+      if (a < P && b < P && (ti != tj || a < b)) A[(int64_t)b * P + a] = make_double2(sRe[tx][r], -sIm[tx][r]);
     }
     __syncthreads();
   }

@@ -288,17 +288,19 @@ class BranchFreeOperator(Operator):
 
     # ------------------------------------------------------- fused path
     def fused_capable(self, psi):
+        from ..nets.cnn import CNN
         from ..nets.rbm import CpxRBM
         from ..nets.sym_wrapper import SymNet
         if isinstance(psi.net, SymNet):
             return psi.net.average == 0 and self.lDim == 2
-        return isinstance(psi.net, CpxRBM) and self.lDim == 2
+        return isinstance(psi.net, (CpxRBM, CNN)) and self.lDim == 2
 
     def get_O_loc_fused(self, samples, psi, logPsiS=None, *args):
-        """O_loc(s) of a CpxRBM (or symmetrised CpxRBM) state without
+        """O_loc(s) of a CpxRBM, symmetrised CpxRBM or CNN state without
         materialising s': one kernel applies every string and forms
-        psi(s')/psi(s) from tanh(theta) and the exp(+-2W) tables
-        (csrc/rbm.cu, csrc/sym_rbm.cu).  With ``logPsiS`` given the result is
+        psi(s')/psi(s) from tanh(theta) and the exp(+-2W) tables (csrc/rbm.cu,
+        csrc/sym_rbm.cu) or from local updates of the CNN's activations
+        (csrc/cnn.cu).  With ``logPsiS`` given the result is
         relative to it, as in base.py:162-164."""
         s = as_configs(samples)
         psi.init_net(s)
@@ -307,11 +309,17 @@ class BranchFreeOperator(Operator):
         N, L = flat.shape
         params = psi.params_for()
         prec = psi.net._prec(psi.precision)
-        M = int(params["kernel"].shape[1])
         lps = None
         if logPsiS is not None:
             lps = torch.as_tensor(logPsiS).to(device=flat.device, dtype=torch.complex128).reshape(-1).contiguous()
         out = torch.empty(N, dtype=torch.complex128, device=flat.device)
+        from ..nets.cnn import CNN
+        if isinstance(psi.net, CNN):
+            d = psi.net.desc(tuple(s.shape[2:]))
+            _lib.call("vmc_cnn_oloc_fused", prec, _lib.ctypes_ref(d), _lib.ptr(flat), N,
+                      _lib.ptr(psi.net.flat(params, psi.precision)), op, _lib.ptr(lps), _lib.ptr(out), _lib.stream())
+            return out.reshape(s.shape[:2])
+        M = int(params["kernel"].shape[1])
         from ..nets.sym_wrapper import SymNet
         if isinstance(psi.net, SymNet):
             _lib.call("vmc_sym_rbm_oloc_fused", prec, _lib.ptr(flat), N, L, M, _lib.ptr(params["kernel"]),

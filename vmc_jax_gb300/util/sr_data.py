@@ -47,11 +47,16 @@ class RbmData:
 
 
 class DenseData:
-    def __init__(self, psi, flat, precision):
+    """``real=True``: a real-parameter net (O real, stored as complex128 with
+    imaginary part 0; S and F are the real parts, makeReal = Re)."""
+
+    def __init__(self, psi, flat, precision, real=False):
         params = psi.params_for(precision)
-        self.O = psi.net.gradients(params, flat, precision, _lib.VMC_GRAD_COMPACT)
+        layout = _lib.VMC_GRAD_REFERENCE if real else _lib.VMC_GRAD_COMPACT
+        self.O = psi.net.gradients(params, flat, precision, layout)
         self.N, self.P = self.O.shape
         self.device = flat.device
+        self.real = real
 
     def stats(self, w, E, emean, okMean, covOE):
         ws = _lib.Workspace.get(_lib.query("vmc_dense_grad_stats_workspace_bytes", self.N, self.P))
@@ -64,16 +69,19 @@ class DenseData:
 
     def snr_data(self, w, okMean, E, emean, negx, f, fmt, out, out_lo, ld):
         _lib.call("vmc_dense_snr_data", _lib.ptr(self.O), self.P, self.N, self.P, _lib.ptr(w), _lib.ptr(okMean),
-                  _lib.ptr(E), _lib.ptr(emean), negx.real, negx.imag, _lib.ptr(f), fmt, _lib.ptr(out),
-                  _lib.ptr(out_lo), ld, _lib.stream())
+                  _lib.ptr(E), _lib.ptr(emean), negx.real, negx.imag, _lib.ptr(f), int(self.real), fmt,
+                  _lib.ptr(out), _lib.ptr(out_lo), ld, _lib.stream())
 
 
 def producer(psi, flat, precision):
     """The data producer for the network of ``psi`` (None: no complex path)."""
+    from ..nets.cnn import CNN
     from ..nets.rbm import CpxRBM
     from ..nets.sym_wrapper import SymNet
     if isinstance(psi.net, CpxRBM):
         return RbmData(psi, flat, precision)
     if isinstance(psi.net, SymNet):
         return DenseData(psi, flat, precision)
+    if isinstance(psi.net, CNN):
+        return DenseData(psi, flat, precision, real=True)
     return None

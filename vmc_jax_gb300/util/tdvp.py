@@ -121,9 +121,13 @@ class TDVP:
 
     # ========================================== complex (holomorphic) path
     def _complex_capable(self, psi):
-        """CpxRBM and SymNet(CpxRBM) states take the complex P x P pipeline."""
+        """CpxRBM and SymNet(CpxRBM) states take the complex P x P pipeline;
+        a real-parameter CNN takes it with makeReal='real' (S and F real)."""
+        from ..nets.cnn import CNN
         from ..nets.rbm import CpxRBM
         from ..nets.sym_wrapper import SymNet
+        if isinstance(psi.net, CNN):
+            return self.makeRealName == 'real'
         return isinstance(psi.net, (CpxRBM, SymNet))
 
     def _rbm_capable(self, psi, hamiltonian):
@@ -160,6 +164,9 @@ class TDVP:
         data.stats(w, E, emean, okMean, covOE)
         x = complex(self.rhsPrefactor)
         f = (-x) * covOE                       # complex form of F0 (tdvp.py:139)
+        realParams = bool(getattr(data, "real", False))
+        if realParams:                         # makeReal = Re (tdvp.py:140)
+            f = torch.complex(f.real, torch.zeros_like(f.real))
 
         # S = <O^dagger O>_c  (tdvp.py:142)
         shift = float(self.diagonalShift) if (self.diagonalShift > 1e-10 and self.makeRealName != 'imag') else 0.0
@@ -197,9 +204,12 @@ class TDVP:
         self._A, self._shift, self._z, self._covOE = A, shift, z, covOE
         self._leafSizes = [int(q.numel()) for q in psi.params.values()]
         self._complexLast = True
+        self._realParams = realParams
         self.ev_c, self.V, self.VtF, self.snr_c = ev, U, vtf, snr
         self.ElocMean = emean[0]
         self.ElocVar = evar[0]
+        if realParams:
+            return z.real.contiguous(), res[0], res[1]
         return self._realrep(psi, z), res[0], res[1]
 
     def S_dot(self, v):
@@ -211,6 +221,12 @@ class TDVP:
         if not getattr(self, "_complexLast", False):
             return torch.matmul(self.S0, torch.as_tensor(v, device=self.S0.device).to(self.S0.dtype))
         v = torch.as_tensor(v, device=self._A.device).to(torch.float64)
+        if self._realParams:
+            z = v.to(torch.complex128)
+            y = torch.mv(self._A, z)
+            if self._shift:
+                y = y - (self._shift / (1.0 + self._shift)) * self._A.diagonal() * z
+            return y
         zs, start = [], 0
         for n in self._leafSizes:
             zs.append(torch.complex(v[start:start + n], v[start + n:start + 2 * n]))
@@ -302,7 +318,9 @@ class TDVP:
         x = complex(self.rhsPrefactor)
         zF = torch.vdot(z, (-x) * self._covOE)
         err = torch.abs(1. + (zAz - 2. * torch.real(zF)) / self.ElocVar0)
-        if self.makeRealName == 'imag':
+        if self._realParams:
+            spectrum, snr = self.ev_c, self.snr_c
+        elif self.makeRealName == 'imag':
             spectrum = torch.cat([-torch.flip(self.ev_c, [0]), self.ev_c])
             snr = torch.cat([torch.flip(self.snr_c, [0]), self.snr_c])
         else:
