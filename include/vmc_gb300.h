@@ -86,11 +86,11 @@ int vmc_exact_probabilities(const double* log_psi, int64_t num_states, int64_t n
  * ------------------------------------------------------------------------ */
 
 /* Size in bytes of the per-parameter tables used by the fused local-energy
- * and Metropolis kernels (4 complex (L, M) tables). */
+ * and Metropolis kernels (5 complex (L, M) tables and L row sums). */
 size_t vmc_rbm_tables_bytes(int32_t precision, int32_t num_sites, int32_t num_hidden);
 
-/* Fill the tables: cosh(2W), sinh(2W), exp(2W), exp(-2W).  Call after every
- * parameter change. */
+/* Fill the tables: cosh(2W), sinh(2W), exp(2W), exp(-2W), tanh(2W), then
+ * sum_j log cosh(2 W_ij) per row i.  Call after every parameter change. */
 int vmc_rbm_prepare(int32_t precision, int32_t num_sites, int32_t num_hidden, const void* kernel, void* tables,
                     vmc_stream_t stream);
 

@@ -119,7 +119,7 @@ def load(build_if_missing=True):
 
 # kernels launched by one successful call of each entry point
 KERNELS_PER_CALL = {
-    "vmc_exact_basis": 1, "vmc_exact_probabilities": 2, "vmc_mc_probabilities": 2, "vmc_rbm_prepare": 1,
+    "vmc_exact_basis": 1, "vmc_exact_probabilities": 2, "vmc_mc_probabilities": 2, "vmc_rbm_prepare": 2,
     "vmc_rbm_logpsi": 1, "vmc_rbm_gradients": 1, "vmc_rbm_metropolis": 1, "vmc_bf_matrix_elements": 1,
     "vmc_bf_gather": 1, "vmc_oloc_from_sprimes": 1, "vmc_rbm_oloc_fused": 1, "vmc_weighted_mean_var": 3,
     "vmc_rbm_grad_stats": 3, "vmc_rbm_centered_gradients": 1, "vmc_rbm_snr_data": 1, "vmc_gram_to_hermitian": 1,

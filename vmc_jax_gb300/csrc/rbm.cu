@@ -44,6 +44,22 @@ __global__ void rbm_prepare_kernel(const cpx<T>* __restrict__ W, int64_t n, cpx<
     tab[n + t] = T(0.5) * (ep - em);      // sinh 2W
     tab[2 * n + t] = ep;                  // exp 2W
     tab[3 * n + t] = em;                  // exp -2W
+    tab[4 * n + t] = ctanh_(mk(T(2) * w.re, T(2) * w.im));  // tanh 2W
+  }
+}
+
+// row sums sum_j log cosh(2 W_ij) after the five tables (one warp per row i)
+template <typename T>
+__global__ void rbm_prepare_rows_kernel(const cpx<T>* __restrict__ W, int L, int M, cpx<T>* __restrict__ rows) {
+  const int lane = threadIdx.x & 31;
+  for (int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < L; i += gridDim.x * (blockDim.x >> 5)) {
+    cpx<T> s = mk(T(0), T(0));
+    for (int j = lane; j < M; j += 32) {
+      const cpx<T> w = W[(size_t)i * M + j];
+      s = s + log_cosh(mk(T(2) * w.re, T(2) * w.im));
+    }
+    s = warp_sum(s);
+    if (lane == 0) rows[i] = s;
   }
 }
 
@@ -452,7 +468,7 @@ using namespace vmc;
 
 extern "C" size_t vmc_rbm_tables_bytes(int32_t precision, int32_t num_sites, int32_t num_hidden) {
   size_t el = precision == VMC_F32 ? 8 : 16;
-  return 4 * (size_t)num_sites * (size_t)num_hidden * el;
+  return (5 * (size_t)num_sites * (size_t)num_hidden + (size_t)num_sites) * el;
 }
 
 extern "C" int vmc_rbm_prepare(int32_t precision, int32_t num_sites, int32_t num_hidden, const void* kernel,
@@ -462,12 +478,20 @@ extern "C" int vmc_rbm_prepare(int32_t precision, int32_t num_sites, int32_t num
   VMC_REQUIRE(tables, VMC_ERR_INVALID_ARGUMENT, "vmc_rbm_prepare: null tables");
   int64_t n = (int64_t)num_sites * num_hidden;
   int blocks = (int)std::min<int64_t>((n + 255) / 256, 152 * 8);
-  if (precision == VMC_F64)
-    rbm_prepare_kernel<double><<<blocks, 256, 0, as_stream(stream)>>>(
-        reinterpret_cast<const cpx<double>*>(kernel), n, reinterpret_cast<cpx<double>*>(tables));
-  else
+  const int rowBlocks = (num_sites + 7) / 8;
+  if (precision == VMC_F64) {
+    cpx<double>* tab = reinterpret_cast<cpx<double>*>(tables);
+    rbm_prepare_kernel<double><<<blocks, 256, 0, as_stream(stream)>>>(reinterpret_cast<const cpx<double>*>(kernel),
+                                                                      n, tab);
+    rbm_prepare_rows_kernel<double><<<rowBlocks, 256, 0, as_stream(stream)>>>(
+        reinterpret_cast<const cpx<double>*>(kernel), num_sites, num_hidden, tab + 5 * n);
+  } else {
+    cpx<float>* tab = reinterpret_cast<cpx<float>*>(tables);
     rbm_prepare_kernel<float><<<blocks, 256, 0, as_stream(stream)>>>(reinterpret_cast<const cpx<float>*>(kernel), n,
-                                                                    reinterpret_cast<cpx<float>*>(tables));
+                                                                    tab);
+    rbm_prepare_rows_kernel<float><<<rowBlocks, 256, 0, as_stream(stream)>>>(
+        reinterpret_cast<const cpx<float>*>(kernel), num_sites, num_hidden, tab + 5 * n);
+  }
   return check_launch("vmc_rbm_prepare");
 }
 

@@ -494,7 +494,26 @@ __device__ void sym_mc_rebuild(const rbm_params<T>& p, const sym_params& sp, con
   __syncthreads();
 }
 
-template <typename T>
+// per (orbit element, site): 2 * position + flip bit of that position, or -1
+// when the tables are malformed
+__device__ __forceinline__ void sym_build_comb(const sym_params& sp, int L, int16_t* comb) {
+  for (int e = threadIdx.x; e < sp.S * L; e += blockDim.x) {
+    const int t = e / L;
+    const int pi = sp.inv[e];
+    int v = -1;
+    if ((unsigned)pi < (unsigned)L) {
+      const int c = sp.code[(size_t)t * L + pi];
+      if ((unsigned)(c >> 1) < (unsigned)L) v = 2 * pi + (c & 1);
+    }
+    comb[e] = (int16_t)v;
+  }
+}
+
+// r_tau = exp(rowLogC_p) prod_j (1 - sigma tanh(theta_j) tanh(2 W_pj)):
+// cosh(theta + D)/cosh(theta) = cosh 2W (1 - sigma t tanh 2W), the row's
+// cosh product taken out of the loop.  G threads per orbit element, JPT
+// hidden units each (loads hoisted by the unrolled loop), butterfly over G.
+template <typename T, int JPT>
 __global__ void __launch_bounds__(kSymThreads) sym_rbm_metropolis_kernel(
     int32_t* __restrict__ states, int C, rbm_params<T> p, sym_params sp, const cpx<T>* __restrict__ tab, double mu,
     uint64_t seed, uint32_t call, int64_t thermSteps, int64_t sweepSteps, int64_t samplesPerChain, int G,
@@ -511,47 +530,50 @@ __global__ void __launch_bounds__(kSymThreads) sym_rbm_metropolis_kernel(
   cpx<T>* w = reinterpret_cast<cpx<T>*>(smem);
   cpx<T>* rat = w + sp.S;
   cpx<T>* tst = rat + sp.S;
-  int8_t* cfg = reinterpret_cast<int8_t*>(tst + (size_t)sp.S * M);
+  int16_t* comb = reinterpret_cast<int16_t*>(tst + (size_t)sp.S * M);
+  int8_t* cfg = reinterpret_cast<int8_t*>(comb + (((size_t)sp.S * L + 7) & ~(size_t)7));
   int8_t* tcfg = cfg + Lp + warp * Lp;
   int32_t* st = states + (size_t)chain * L;
   for (int i = threadIdx.x; i < L; i += blockDim.x) cfg[i] = (int8_t)st[i];
+  sym_build_comb(sp, L, comb);
   __syncthreads();
   sym_mc_rebuild(p, sp, cfg, tcfg, tst, w, warp, lane);
 
   const size_t LM = (size_t)L * M;
-  const cpx<T>* tC = tab;
-  const cpx<T>* tS = tab + LM;
+  const cpx<T>* tT = tab + 4 * LM;
+  const cpx<T>* rowLogC = tab + 5 * LM;
   unsigned long long accepted = 0;
   const int64_t total = thermSteps + sweepSteps * samplesPerChain;
   for (int64_t step = 0; step < total; ++step) {
     const mc_draw d = metropolis_draw(seed, call, (uint32_t)step, (uint32_t)chain, L);
     const int i = d.site;
-    // G threads per orbit element: partial products over j = sub, sub + G, ..
-    // then a butterfly over the G lanes of the group.  The trip count is the
-    // same for every thread (t0 loop), so the shuffles see full warps.
+    // same trip counts on every thread: the group butterflies see full warps
     for (int t0 = 0; t0 < sp.S; t0 += nGroups) {
       const int t = t0 + gid;
       const bool active = t < sp.S;
-      const int pi = active ? sp.inv[(size_t)t * L + i] : 0;
+      const int pc = active ? comb[t * L + i] : 0;
+      const int pi = pc >> 1;
+      const T sg = (cfg[i] ^ (pc & 1)) ? T(1) : T(-1);
       scaled_cpx<T> prod;
       prod.m = mk(T(1), T(0));
       prod.ex = 0;
-      if (!active) {
-      } else if ((unsigned)pi < (unsigned)L) {
-        const int c = sp.code[(size_t)t * L + pi];
-        const T sg = (cfg[i] ^ (c & 1)) ? T(1) : T(-1);
-        const cpx<T>* rc = tC + (size_t)pi * M;
-        const cpx<T>* rs = tS + (size_t)pi * M;
+      if (active && pc >= 0) {
+        const cpx<T>* rt = tT + (size_t)pi * M;
         const cpx<T>* tt = tst + (size_t)t * M;
-        int cnt = 0;
-        for (int j = sub; j < M; j += G) {
-          prod.m = prod.m * (rc[j] - sg * (tt[j] * rs[j]));
-          if (++cnt == 8) {
-            renorm(prod);
-            cnt = 0;
-          }
+        cpx<T> tv[JPT], rv[JPT];
+#pragma unroll
+        for (int q = 0; q < JPT; ++q) {
+          const int j = sub + q * G;
+          tv[q] = j < M ? tt[j] : mk(T(0), T(0));
+          rv[q] = j < M ? rt[j] : mk(T(0), T(0));
         }
-      } else {
+#pragma unroll
+        for (int q = 0; q < JPT; ++q) {
+          const cpx<T> f = tv[q] * rv[q];
+          prod.m = prod.m * mk(T(1) - sg * f.re, -sg * f.im);
+          if ((q & 7) == 7) renorm(prod);
+        }
+      } else if (active) {
         prod.m = mk(T(nan("")), T(nan("")));
       }
       renorm(prod);
@@ -562,6 +584,15 @@ __global__ void __launch_bounds__(kSymThreads) sym_rbm_metropolis_kernel(
         prod = mul(prod, o);
       }
       if (active && sub == 0) {
+        if (pc >= 0) {
+          // times exp(rowLogC_p) = 2^e2 * (exp(re - e2 ln 2) (cos im, sin im))
+          const cpx<T> lc = rowLogC[pi];
+          const T e2 = floor(lc.re * T(1.4426950408889634));
+          scaled_cpx<T> cr;
+          cr.m = cexp_(mk(lc.re - e2 * T(0.6931471805599453), lc.im));
+          cr.ex = (int)e2;
+          prod = mul(prod, cr);
+        }
         // ratios beyond the float range saturate (they decide acceptance alone)
         const int lim = sizeof(T) == sizeof(double) ? 2000 : 120;
         const int e = max(-lim, min(lim, prod.ex));
@@ -597,16 +628,16 @@ __global__ void __launch_bounds__(kSymThreads) sym_rbm_metropolis_kernel(
     if (sAcc) {
       const cpx<T> R = sR;
       for (int t = gid; t < sp.S; t += nGroups) {
-        const int pi = sp.inv[(size_t)t * L + i];
-        if ((unsigned)pi < (unsigned)L) {
-          const int c = sp.code[(size_t)t * L + pi];
-          const T sg = (cfg[i] ^ (c & 1)) ? T(1) : T(-1);
-          const cpx<T>* rc = tC + (size_t)pi * M;
-          const cpx<T>* rs = tS + (size_t)pi * M;
+        const int pc = comb[t * L + i];
+        if (pc >= 0) {
+          const T sg = (cfg[i] ^ (pc & 1)) ? T(1) : T(-1);
+          const cpx<T>* rt = tT + (size_t)(pc >> 1) * M;
           cpx<T>* tt = tst + (size_t)t * M;
+          // tanh(theta + D) = (t - sigma tanh 2W) / (1 - sigma t tanh 2W)
           for (int j = sub; j < M; j += G) {
-            const cpx<T> cj = rc[j], sj = rs[j], tj = tt[j];
-            tt[j] = cdiv(tj * cj - sg * sj, cj - sg * (tj * sj));
+            const cpx<T> tj = tt[j], rj = rt[j];
+            const cpx<T> f = tj * rj;
+            tt[j] = cdiv(mk(tj.re - sg * rj.re, tj.im - sg * rj.im), mk(T(1) - sg * f.re, -sg * f.im));
           }
         }
         if (sub == 0 && sp.avg == VMC_SYM_EXP) w[t] = cdiv(w[t] * rat[t], R);
@@ -795,6 +826,28 @@ extern "C" int vmc_sym_rbm_oloc_fused(int32_t precision, const int32_t* configs,
                                   oloc);
 }
 
+template <typename T, int JPT>
+static void launch_sym_mc(int C, size_t smem, cudaStream_t st, int32_t* states, rbm_params<T> p, sym_params sp,
+                          const void* tables, double mu, uint64_t seed, uint32_t call, int64_t therm, int64_t sweep,
+                          int64_t spc, int G, int32_t* out, void* counters) {
+  set_smem((const void*)sym_rbm_metropolis_kernel<T, JPT>, smem);
+  sym_rbm_metropolis_kernel<T, JPT><<<C, kSymThreads, smem, st>>>(
+      states, C, p, sp, reinterpret_cast<const cpx<T>*>(tables), mu, seed, call, therm, sweep, spc, G, out,
+      reinterpret_cast<unsigned long long*>(counters));
+}
+
+template <typename T>
+static int dispatch_sym_mc(int jpt, int C, size_t smem, cudaStream_t st, int32_t* states, rbm_params<T> p,
+                           sym_params sp, const void* tables, double mu, uint64_t seed, uint32_t call, int64_t therm,
+                           int64_t sweep, int64_t spc, int G, int32_t* out, void* counters) {
+  if (jpt <= 2) launch_sym_mc<T, 2>(C, smem, st, states, p, sp, tables, mu, seed, call, therm, sweep, spc, G, out, counters);
+  else if (jpt <= 4) launch_sym_mc<T, 4>(C, smem, st, states, p, sp, tables, mu, seed, call, therm, sweep, spc, G, out, counters);
+  else if (jpt <= 8) launch_sym_mc<T, 8>(C, smem, st, states, p, sp, tables, mu, seed, call, therm, sweep, spc, G, out, counters);
+  else if (jpt <= 16) launch_sym_mc<T, 16>(C, smem, st, states, p, sp, tables, mu, seed, call, therm, sweep, spc, G, out, counters);
+  else launch_sym_mc<T, 32>(C, smem, st, states, p, sp, tables, mu, seed, call, therm, sweep, spc, G, out, counters);
+  return VMC_OK;
+}
+
 extern "C" int vmc_sym_rbm_metropolis(int32_t precision, int32_t* states, int32_t num_chains, int32_t num_sites,
                                       int32_t num_hidden, const void* kernel, const void* bias, const void* tables,
                                       const vmc_sym_desc* sym, double mu, uint64_t seed, uint32_t call_index,
@@ -811,25 +864,26 @@ extern "C" int vmc_sym_rbm_metropolis(int32_t precision, int32_t* states, int32_
   VMC_REQUIRE(mu >= 0.0 && mu <= 2.0, VMC_ERR_INVALID_ARGUMENT, "vmc_sym_rbm_metropolis: mu=%g outside [0, 2]", mu);
   const int Lp = (num_sites + 15) & ~15;
   const size_t el = precision == VMC_F64 ? 16 : 8;
-  const size_t smem = (2 + (size_t)num_hidden) * sym->num_sym * el + (size_t)(1 + kSymWarps) * Lp;
+  VMC_REQUIRE(num_hidden <= 32 * 32 && num_sites <= 16383, VMC_ERR_UNSUPPORTED,
+              "vmc_sym_rbm_metropolis: M=%d > 1024 or L=%d > 16383", num_hidden, num_sites);
+  const size_t smem = (2 + (size_t)num_hidden) * sym->num_sym * el + ((((size_t)sym->num_sym * num_sites + 7) & ~(size_t)7) * 2) +
+                      (size_t)(1 + kSymWarps) * Lp;
   VMC_REQUIRE(smem <= kSmemLimit, VMC_ERR_UNSUPPORTED,
               "vmc_sym_rbm_metropolis: %d orbit elements x %d hidden units do not fit in shared memory", sym->num_sym,
               num_hidden);
   cudaStream_t st = as_stream(stream);
   const sym_params sp = make_sym(sym);
-  const int G = group_size(sym->num_sym, num_hidden);
-  if (precision == VMC_F64) {
-    set_smem((const void*)sym_rbm_metropolis_kernel<double>, smem);
-    sym_rbm_metropolis_kernel<double><<<num_chains, kSymThreads, smem, st>>>(
-        states, num_chains, make_params<double>(kernel, bias, num_sites, num_hidden), sp,
-        reinterpret_cast<const cpx<double>*>(tables), mu, seed, call_index, therm_steps, sweep_steps, samples_per_chain,
-        G, configs_out, reinterpret_cast<unsigned long long*>(counters));
-  } else {
-    set_smem((const void*)sym_rbm_metropolis_kernel<float>, smem);
-    sym_rbm_metropolis_kernel<float><<<num_chains, kSymThreads, smem, st>>>(
-        states, num_chains, make_params<float>(kernel, bias, num_sites, num_hidden), sp,
-        reinterpret_cast<const cpx<float>*>(tables), mu, seed, call_index, therm_steps, sweep_steps, samples_per_chain,
-        G, configs_out, reinterpret_cast<unsigned long long*>(counters));
-  }
+  int G = group_size(sym->num_sym, num_hidden);
+  while (G < 32 && (num_hidden + G - 1) / G > 16) G <<= 1;
+  const int jpt = (num_hidden + G - 1) / G;
+  if (precision == VMC_F64)
+    rc = dispatch_sym_mc<double>(jpt, num_chains, smem, st, states, make_params<double>(kernel, bias, num_sites, num_hidden),
+                                 sp, tables, mu, seed, call_index, therm_steps, sweep_steps, samples_per_chain, G,
+                                 configs_out, counters);
+  else
+    rc = dispatch_sym_mc<float>(jpt, num_chains, smem, st, states, make_params<float>(kernel, bias, num_sites, num_hidden),
+                                sp, tables, mu, seed, call_index, therm_steps, sweep_steps, samples_per_chain, G,
+                                configs_out, counters);
+  if (rc) return rc;
   return check_launch("vmc_sym_rbm_metropolis");
 }

@@ -175,7 +175,11 @@ class TDVP:
 
         # eigendecomposition (tdvp.py:153-171), FP64 on the GPU
         TIMER.mark("eigh")
-        ev, U = torch.linalg.eigh(A)
+        if realParams:  # S real symmetric: the real eigensolver, vectors as complex
+            ev, U = torch.linalg.eigh(A.real.contiguous())
+            U = U.to(torch.complex128)
+        else:
+            ev, U = torch.linalg.eigh(A)
         if U.stride(0) != 1:
             U = U.mT.contiguous().mT
         vtf = torch.empty(P, dtype=torch.complex128, device=dev)
