@@ -562,13 +562,31 @@ def quench_bench(args):
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
         E = np.array(E)
+        if prec == "mixed":
+            # estimator error of the FP32 kernels: E on the same samples at the
+            # final parameters with FP32 and with FP64 kernels
+            smp_chk = V.sampler.MCSampler(psi, (L,), 11, updateProposer=V.sampler.propose_spin_flip,
+                                          numChains=1024, numSamples=8192, thermalizationSweeps=8, sweepSteps=L)
+            psi.precision = "fp64"
+            psi._touch()
+            cfgs, _, pw = smp_chk.sample()
+            e_pair = {}
+            for kp in ("fp32", "fp64"):
+                psi.precision = kp
+                psi._touch()
+                el = H.get_O_loc(cfgs, psi, None)
+                e_pair[kp] = float(torch.real(torch.sum(el * pw)))
+            psi.precision = "fp32"
+            psi._touch()
+            same_sample_err = abs(e_pair["fp32"] - e_pair["fp64"]) / abs(e_pair["fp64"])
         res[prec] = {"steps": len(E), "t_end": t, "wall_s": wall, "E0": float(E[0]), "stopped_early": t < args.quench,
                      "drift": float(np.max(np.abs(E - E[0])) / abs(E[0])), "E": E.tolist(), "t": times}
     emit({"metric": "XXZ quench energy drift, mixed vs FP64 solve", "workload": "xxz48_rbm96_quench",
           "config": {"L": L, "M": M, "delta": delta, "num_samples": 8192,
                      "integrator": "AdaptiveHeun tol 1e-4, S-metric error norm", "t_end": args.quench,
                      "max_steps": args.quench_steps, "max_wall_s": args.quench_wall},
-          "data": "synthetic (seeded)", **res})
+          "data": "synthetic (seeded)",
+          "energy_rel_err_fp32_vs_fp64_same_samples": same_sample_err, **res})
 
 
 def serve_bench(args):

@@ -332,8 +332,12 @@ static cnn_local make_local(const cnn_geom& g) {
   return lc;
 }
 
+// v mod n for -2n <= v < 3n (every use below stays in that range), without
+// an integer division
 __device__ __forceinline__ int wrap(int v, int n) {
-  v %= n;
+  v = v >= n ? v - n : v;
+  v = v >= n ? v - n : v;
+  v = v < 0 ? v + n : v;
   return v < 0 ? v + n : v;
 }
 
@@ -524,8 +528,14 @@ __global__ void cnn_metropolis_local_kernel(int32_t* __restrict__ states, int C,
   for (int64_t step = 0; step < total; ++step) {
     const mc_draw d = metropolis_draw(seed, call, (uint32_t)step, (uint32_t)chain, g.sites);
     const T delta = warp_local_delta(g, lc, prm, cfg, a, scr, d.site, lane);
-    const double P = exp(mu * (double)delta);
-    if (d.u64() < P) {
+    // accept iff u < exp(mu delta): FP64 rule in the FP64 kernel (replayed by
+    // the parity test), FP32 in the FP32 kernel
+    bool acc;
+    if (sizeof(T) == sizeof(double))
+      acc = d.u64() < exp(mu * (double)delta);
+    else
+      acc = d.u32() < expf((float)mu * (float)delta);
+    if (acc) {
       warp_local_commit(g, lc, cfg, a, scr, d.site, lane);
       ++accepted;
     }

@@ -2,7 +2,9 @@
 //   log psi(s) = avg_tau log psi_RBM(tau(s)),
 // avg = log sum_tau f_tau exp(.) (avgFun_Coefficients_Exp, sym_wrapper.py:7-9)
 // or the mean (avgFun_Coefficients_Log, 12-13).  One block per configuration
-// (or per chain), one warp per orbit element at a time.
+// (or per chain); log psi and gradients take one warp per orbit element at a
+// time, the per-proposal / per-string ratio products G threads per orbit
+// element (a power of two <= 32) with a butterfly over the group.
 //
 // The orbit arrives as codes (S, L): code = 2 src + flip, tau(s)_i =
 // s_src xor flip, and its inverse (S, L): inv[tau][j] = the position i with
@@ -468,9 +470,9 @@ __global__ void __launch_bounds__(kSymThreads) sym_rbm_oloc_fused_kernel(
 //   psi(s')/psi(s) = sum_tau w_tau r_tau          (Exp)
 //   |psi(s')/psi(s)| = prod_tau |r_tau|^(1/S)      (Log).
 // Acceptance iff u < |psi(s')/psi(s)|^mu (sampler.py:335-340).  On acceptance
-// tanh(theta + D) = (t cosh 2W - sigma sinh 2W) / (cosh 2W - sigma t sinh 2W)
-// and w_tau <- w_tau r_tau / R.  Every sweepSteps steps the state is rebuilt
-// from the configuration, so rounding does not accumulate.
+// tanh(theta + D) = (t - sigma tanh 2W) / (1 - sigma t tanh 2W) and
+// w_tau <- w_tau r_tau / R.  Every sweepSteps steps the state is rebuilt from
+// the configuration, so rounding does not accumulate.
 template <typename T>
 __device__ void sym_mc_rebuild(const rbm_params<T>& p, const sym_params& sp, const int8_t* cfg, int8_t* tcfg,
                                cpx<T>* tst, cpx<T>* w, int warp, int lane) {
