@@ -715,16 +715,21 @@ def main():
         flops = 4.0 * Ns * P * (P + 1)  # Hermitian S build, 8 flop per complex MAC
         peak = peaks.get("bf16_tflops_sustained", 1700.0)
         ach = flops / t / 1e12
-        traffic = None
-        try:
-            with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
-                traffic = json.load(f).get("tc_gemm_gram_per_launch_bytes")
-        except Exception:
-            pass
+        # DRAM traffic of one launch, scaled from the ncu capture of the same
+        # kernel at rows 8192, K 16384 (profiles/tc_gemm_gram_rows8192_k16384.md:
+        # 4.689 GB read + 0.123 GB written over 1056 tiles of 128 x 256): per
+        # tile the operand panels grow with K, the FP32 tile write does not
+        R = 2 * P
+        tilesM, tilesN = (R + 127) // 128, (R + 255) // 256
+        tiles = sum(min(tilesM, 2 * tn + 2) for tn in range(tilesN))
+        traffic = tiles * (4.688826e9 / 1056 * (Ns / 16384.0) + 0.122841e9 / 1056)
         roofline = {"kernel": "tc_gemm_kernel (S build, BF16x3 split, tcgen05)", "bound": "tensor",
                     "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
                     "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained (of measured)",
-                    "traffic": traffic, "algorithmic_flops_per_launch": flops,
+                    "traffic": traffic,
+                    "traffic_source": "ncu dram__bytes_read+write of the rows-8192 K-16384 capture, scaled by tiles "
+                                      "and K",
+                    "algorithmic_flops_per_launch": flops,
                     "hardware_flops_per_launch": 3 * 2.0 * Ns * (2 * P) ** 2 / 2,
                     "launch_ms": t * 1e3}
     out = {"metric": "TDVP steps/s", "value": aggregate_steps_per_s(args.steps, world, ms), "unit": "steps/s",

@@ -58,6 +58,39 @@ def test_invalid_arguments_are_rejected_on_the_host():
     assert rc == 5
 
 
+def test_symnet_cnn_dense_arguments_are_rejected_on_the_host():
+    from vmc_jax_gb300.nets.sym_wrapper import SymDesc
+    lib = L.load()
+    p = ctypes.c_void_p(16)
+    # SymNet: missing descriptor, empty orbit, unknown average
+    rc = lib.vmc_sym_rbm_logpsi(0, p, 1, 4, 2, p, None, None, p, None)
+    assert rc == 1 and b"symmetry descriptor" in lib.vmc_last_error_string()
+    d = SymDesc(0, 0, 16, 16, 16)
+    rc = lib.vmc_sym_rbm_logpsi(0, p, 1, 4, 2, p, None, ctypes.addressof(d), p, None)
+    assert rc == 2
+    d = SymDesc(4, 7, 16, 16, 16)
+    rc = lib.vmc_sym_rbm_gradients(0, p, 1, 4, 2, p, None, ctypes.addressof(d), 0, p, None)
+    assert rc == 1 and b"average" in lib.vmc_last_error_string()
+    # the fused SymNet estimator exists for the Exp average only
+    d = SymDesc(4, 1, 16, 16, 16)
+    op = L.BfOperator(num_ops=2, max_len=2, local_dim=2, num_diag=0, idx=16, map=16, mat_els=16, fermi=16,
+                      prefactor=16, diag=None)
+    rc = lib.vmc_sym_rbm_oloc_fused(0, p, 1, 4, 2, p, None, p, ctypes.addressof(d), ctypes.byref(op), None, p, None)
+    assert rc == 2 and b"Exp" in lib.vmc_last_error_string()
+    # SymNet sampler: orbit x hidden units beyond shared memory
+    d = SymDesc(4096, 0, 16, 16, 16)
+    rc = lib.vmc_sym_rbm_metropolis(1, p, 4, 8, 1024, p, None, p, ctypes.addressof(d), 2.0, 1, 0, 8, 8, 1, p, p,
+                                    None)
+    assert rc == 2 and b"shared memory" in lib.vmc_last_error_string()
+    # dense producers: leading dimension and workspace checks
+    rc = lib.vmc_dense_centered_gradients(p, 4, 8, 4, p, p, 0, p, None, 2, None)
+    assert rc == 1 and b"leading dimension" in lib.vmc_last_error_string()
+    rc = lib.vmc_dense_grad_stats(p, 4, 8, 4, p, p, p, p, p, None, 0, None)
+    assert rc == 5
+    # CNN fused estimator: operator validated before any launch
+    assert lib.vmc_cnn_oloc_fused(0, None, p, 1, p, ctypes.byref(op), None, p, None) == 1
+
+
 @pytest.mark.parametrize("seed,call,step,L_", [(0, 0, 0, 10), (0x123456789ABCDEF, 3, 17, 64), (7, 9, 12345, 100)])
 def test_philox_stream_matches_oracle(seed, call, step, L_):
     lib = L.load()
