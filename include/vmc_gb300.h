@@ -301,9 +301,14 @@ int vmc_tdvp_snr(const double* vtf, int32_t colsq_precision, const void* colsq, 
 
 /* The regularised pseudo-inverse cutoff loop (tdvp.py:191-209) on the
  * device: pinv (n) and result[3] = {residual, cutoff used, iterations}.
- * snr NULL = exact sampling (no SNR factor). ev ascending. */
+ * snr NULL = exact sampling (no SNR factor). ev ascending.  Every candidate
+ * cutoff is evaluated in parallel and the loop's stopping rule applied to
+ * the residuals; workspace: vmc_tdvp_regularize_workspace_bytes(n,
+ * pinv_cutoff) bytes. */
+size_t vmc_tdvp_regularize_workspace_bytes(int32_t n, double pinv_cutoff);
 int vmc_tdvp_regularize(const double* ev, const double* vtf, const double* snr, int32_t n, double pinv_cutoff,
-                        double pinv_tol, double snr_tol, double* pinv, double* result, vmc_stream_t stream);
+                        double pinv_tol, double snr_tol, double* pinv, double* result, void* workspace,
+                        size_t workspace_bytes, vmc_stream_t stream);
 
 /* ------------------------------------------------------------------------
  * Split-precision BF16 contractions on the tcgen05 tensor cores (FP32

@@ -123,7 +123,7 @@ KERNELS_PER_CALL = {
     "vmc_rbm_logpsi": 1, "vmc_rbm_gradients": 1, "vmc_rbm_metropolis": 1, "vmc_bf_matrix_elements": 1,
     "vmc_bf_gather": 1, "vmc_oloc_from_sprimes": 1, "vmc_rbm_oloc_fused": 1, "vmc_weighted_mean_var": 3,
     "vmc_rbm_grad_stats": 3, "vmc_rbm_centered_gradients": 1, "vmc_rbm_snr_data": 1, "vmc_gram_to_hermitian": 1,
-    "vmc_zgemv": 2, "vmc_tdvp_snr": 1, "vmc_tdvp_regularize": 1, "vmc_gram_bf16x3": 1,
+    "vmc_zgemv": 2, "vmc_tdvp_snr": 1, "vmc_tdvp_regularize": 3, "vmc_gram_bf16x3": 1,
     "vmc_gemm_bf16x3_colsq": 2, "vmc_eigvec_bf16x2": 1, "vmc_cnn_logpsi": 1, "vmc_cnn_gradients": 1,
     "vmc_cnn_metropolis": 1, "vmc_rbm_vjp": 4, "vmc_rbm_grad_stats_noalloc": 3,
     "vmc_rbm_metropolis_devcall": 2, "vmc_sym_rbm_logpsi": 1, "vmc_sym_rbm_gradients": 1,

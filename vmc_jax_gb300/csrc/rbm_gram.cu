@@ -68,20 +68,42 @@ struct data_args {
   void* out2;              // lo plane for BF16X2
 };
 
-// value of column k (complex) for tile row r
+// Column k of the (bias | kernel) layout as (in bias, row i, hidden unit j),
+// advanced by a fixed stride without integer division per element.
+struct col_pos {
+  bool bias;
+  int i, j;
+  __device__ __forceinline__ void set(int k, int M, bool hasBias) {
+    const int P0 = hasBias ? M : 0;
+    bias = k < P0;
+    if (bias) {
+      i = 0;
+      j = k;
+    } else {
+      i = (k - P0) / M;
+      j = (k - P0) - i * M;
+    }
+  }
+  __device__ __forceinline__ void advance(int step, int M) {
+    j += step;
+    if (bias && j >= M) {
+      bias = false;
+      j -= M;
+      i = 0;
+    }
+    while (j >= M) {
+      j -= M;
+      ++i;
+    }
+  }
+};
+
+// value of column k (position c) for tile row r
 template <typename T>
 __device__ __forceinline__ cpx<double> data_value(const data_args& a, const cpx<T>* tt, const int8_t* sg, int r,
-                                                  int64_t n, int k, double sw) {
-  const int P0 = a.hasBias ? a.M : 0;
-  cpx<T> o;
-  if (k < P0) {
-    o = tt[(size_t)r * a.M + k];
-  } else {
-    const int kk = k - P0;
-    const int i = kk / a.M, j = kk - (kk / a.M) * a.M;
-    cpx<T> t = tt[(size_t)r * a.M + j];
-    o = sg[r * a.L + i] ? t : mk(-t.re, -t.im);
-  }
+                                                  int64_t n, int k, const col_pos& c, double sw) {
+  cpx<T> o = tt[(size_t)r * a.M + c.j];
+  if (!c.bias && !sg[r * a.L + c.i]) o = mk(-o.re, -o.im);
   const double2 mu = a.okMean[k];
   cpx<double> d = mk((double)o.re - mu.x, (double)o.im - mu.y);
   if (a.eloc) {
@@ -114,8 +136,10 @@ __global__ void __launch_bounds__(256) rbm_data_kernel(const int32_t* __restrict
     const int64_t n = n0 + r;
     if (n < a.N) {
       const double sw = sqrt(a.w[n]);
-      for (int k = cg; k < P; k += ncg) {
-        cpx<double> v = data_value<T>(a, tt, sg, r, n, k, sw);
+      col_pos c;
+      c.set(cg, a.M, a.hasBias);
+      for (int k = cg; k < P; k += ncg, c.advance(ncg, a.M)) {
+        cpx<double> v = data_value<T>(a, tt, sg, r, n, k, c, sw);
         float vr = (float)v.re, vi = (float)v.im;
         __nv_bfloat16 hr = __float2bfloat16_rn(vr), hi_ = __float2bfloat16_rn(vi);
         hi[(size_t)k * a.ld + n] = hr;
@@ -131,8 +155,10 @@ __global__ void __launch_bounds__(256) rbm_data_kernel(const int32_t* __restrict
     const int64_t n = n0 + r;
     if (n >= a.N) break;
     const double sw = sqrt(a.w[n]);
-    for (int k = tid; k < P; k += blockDim.x) {
-      cpx<double> v = data_value<T>(a, tt, sg, r, n, k, sw);
+    col_pos c;
+    c.set(tid, a.M, a.hasBias);
+    for (int k = tid; k < P; k += blockDim.x, c.advance(blockDim.x, a.M)) {
+      cpx<double> v = data_value<T>(a, tt, sg, r, n, k, c, sw);
       if (a.format == VMC_DATA_C128) {
         reinterpret_cast<double2*>(a.out)[n * a.ld + k] = make_double2(v.re, v.im);
       } else if (a.format == VMC_DATA_C64) {

@@ -124,48 +124,101 @@ __global__ void gemv_reduce_kernel(const double2* __restrict__ part, int chunks,
 //     cutoff *= 0.8; reg = 1/(1 + (max(cutoff,pinvCutoff)/|ev/ev_max|)^6) [* 1/(1+(snrTol/snr)^6)]
 //     pinvEv = invEv * reg; residual = ||(pinvEv ev - 1) VtF|| / ||F||
 // out: pinv (n), result[0] = residual, result[1] = max(cutoff, pinvCutoff).
-__global__ void tdvp_regularize_kernel(const double* __restrict__ ev, const double2* __restrict__ vtf,
-                                       const double* __restrict__ snr, int n, double pinvCutoff,
-                                       double pinvTol, double snrTol, double* __restrict__ pinv,
-                                       double* __restrict__ result, int maxIter) {
+// The loop's iterations are independent given their cutoff, so every
+// candidate cutoff c_m = 1e-2 * 0.8^m (formed by the same repeated products)
+// is evaluated at once: blocks (element chunk, m) write partial sums of
+// d^2 |VtF|^2, one block picks the first m whose residual <= pinvTol (or the
+// last), and a third kernel writes pinv for that m.  The partial sums are
+// added in a fixed order.
+constexpr int kRegChunk = 2048;
+constexpr int kRegMaxIter = 4096;
+
+__device__ __forceinline__ double reg_cutoff(int m) {
+  double c = 1e-2;
+  for (int q = 0; q < m; ++q) c *= 0.8;
+  return c;
+}
+
+__device__ __forceinline__ double reg_pinv(double e, double evMax, double c, const double* snr, double snrTol,
+                                           int k) {
+  const double rel = fabs(e / evMax);
+  const double inv = rel > 1e-14 ? 1.0 / e : 0.0;
+  const double q = c / rel;
+  const double q2 = q * q;
+  double reg = 1.0 / (1.0 + q2 * q2 * q2);
+  if (snr) {
+    const double sq = snrTol / snr[k];
+    const double s2 = sq * sq;
+    reg *= 1.0 / (1.0 + s2 * s2 * s2);
+  }
+  return inv * reg;
+}
+
+__global__ void __launch_bounds__(256) tdvp_reg_partial_kernel(const double* __restrict__ ev,
+                                                               const double2* __restrict__ vtf,
+                                                               const double* __restrict__ snr, int n,
+                                                               double pinvCutoff, double snrTol,
+                                                               double* __restrict__ part, int chunks) {
+  const int chunk = blockIdx.x, m = blockIdx.y + 1;
+  const double c0 = reg_cutoff(m);
+  const double c = c0 > pinvCutoff ? c0 : pinvCutoff;
+  const double evMax = ev[n - 1];  // ev ascending: ev[-1] of the reference
+  double acc = 0.0;
+  const int k1 = min(n, (chunk + 1) * kRegChunk);
+  for (int k = chunk * kRegChunk + threadIdx.x; k < k1; k += blockDim.x) {
+    const double e = ev[k];
+    const double d = reg_pinv(e, evMax, c, snr, snrTol, k) * e - 1.0;
+    acc += d * d * abs2(mk(vtf[k].x, vtf[k].y));
+  }
+  acc = block_sum(acc);
+  if (threadIdx.x == 0) part[(size_t)(m - 1) * chunks + chunk] = acc;
+}
+
+// scalars: [0] chosen m (as double), [1] its cutoff
+__global__ void tdvp_reg_select_kernel(const double2* __restrict__ vtf, int n, const double* __restrict__ part,
+                                       int chunks, int M, double pinvCutoff, double pinvTol,
+                                       double* __restrict__ result, double* __restrict__ scal) {
   double fn = 0.0;
   for (int k = threadIdx.x; k < n; k += blockDim.x) fn += abs2(mk(vtf[k].x, vtf[k].y));
   // ||F||^2 = sum_k |u_k^H f|^2 (U unitary)
   fn = block_sum(fn);
+  if (threadIdx.x != 0) return;
   const double Fnorm = sqrt(fn);
-  const double evMax = ev[n - 1];  // ev ascending: ev[-1] of the reference
   double residual = 1.0, cutoff = 1e-2;
-  int it = 0;
-  while (residual > pinvTol && cutoff > pinvCutoff && it < maxIter) {
-    ++it;
+  int m = 0;
+  // the reference loop: while residual > pinvTol and cutoff > pinvCutoff
+  while (residual > pinvTol && cutoff > pinvCutoff && m < M) {
+    ++m;
     cutoff *= 0.8;
-    const double c = cutoff > pinvCutoff ? cutoff : pinvCutoff;
     double acc = 0.0;
-    for (int k = threadIdx.x; k < n; k += blockDim.x) {
-      const double e = ev[k];
-      const double rel = fabs(e / evMax);
-      const double inv = rel > 1e-14 ? 1.0 / e : 0.0;
-      const double q = c / rel;
-      const double q2 = q * q;
-      double reg = 1.0 / (1.0 + q2 * q2 * q2);
-      if (snr) {
-        const double s = snrTol / snr[k];
-        const double s2 = s * s;
-        reg *= 1.0 / (1.0 + s2 * s2 * s2);
-      }
-      const double pv = inv * reg;
-      pinv[k] = pv;
-      const double d = pv * e - 1.0;
-      acc += d * d * abs2(mk(vtf[k].x, vtf[k].y));
-    }
-    acc = block_sum(acc);
+    for (int q = 0; q < chunks; ++q) acc += part[(size_t)(m - 1) * chunks + q];
     residual = sqrt(acc) / Fnorm;
   }
-  if (threadIdx.x == 0) {
-    result[0] = residual;
-    result[1] = cutoff > pinvCutoff ? cutoff : pinvCutoff;
-    result[2] = (double)it;
+  const double c = cutoff > pinvCutoff ? cutoff : pinvCutoff;
+  result[0] = residual;
+  result[1] = c;
+  result[2] = (double)m;
+  scal[0] = (double)m;
+  scal[1] = c;
+}
+
+__global__ void tdvp_reg_write_kernel(const double* __restrict__ ev, const double* __restrict__ snr, int n,
+                                      double snrTol, const double* __restrict__ scal, double* __restrict__ pinv) {
+  const double c = scal[1];
+  const double evMax = ev[n - 1];
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+    pinv[k] = reg_pinv(ev[k], evMax, c, snr, snrTol, k);
+}
+
+// iterations the loop can run for pinvCutoff (host side, same products)
+static int reg_iterations(double pinvCutoff) {
+  double c = 1e-2;
+  int m = 0;
+  while (c > pinvCutoff && m < kRegMaxIter) {
+    c *= 0.8;
+    ++m;
   }
+  return m;
 }
 
 // snr_k = sqrt(|N |VtF_k|^2 / rhoVar_k|) with rhoVar_k = colsq[k] + colsq[P+k]
@@ -227,12 +280,34 @@ extern "C" int vmc_zgemv(int32_t adjoint, const double* U, int64_t ld, int32_t n
   return check_launch("vmc_zgemv");
 }
 
+extern "C" size_t vmc_tdvp_regularize_workspace_bytes(int32_t n, double pinv_cutoff) {
+  const int chunks = (n + kRegChunk - 1) / kRegChunk;
+  const int M = reg_iterations(pinv_cutoff);
+  return ((size_t)(M > 0 ? M : 1) * chunks + 2) * sizeof(double) + 256;
+}
+
 extern "C" int vmc_tdvp_regularize(const double* ev, const double* vtf, const double* snr, int32_t n,
                                    double pinv_cutoff, double pinv_tol, double snr_tol, double* pinv, double* result,
-                                   vmc_stream_t stream) {
+                                   void* workspace, size_t workspace_bytes, vmc_stream_t stream) {
   VMC_REQUIRE(ev && vtf && pinv && result && n > 0, VMC_ERR_INVALID_ARGUMENT, "vmc_tdvp_regularize: bad arguments");
-  tdvp_regularize_kernel<<<1, 1024, 0, as_stream(stream)>>>(ev, reinterpret_cast<const double2*>(vtf), snr, n,
-                                                          pinv_cutoff, pinv_tol, snr_tol, pinv, result, 100000);
+  const size_t need = vmc_tdvp_regularize_workspace_bytes(n, pinv_cutoff);
+  VMC_REQUIRE(workspace && workspace_bytes >= need, VMC_ERR_WORKSPACE,
+              "vmc_tdvp_regularize: workspace of %zu bytes needed", need);
+  const int chunks = (n + kRegChunk - 1) / kRegChunk;
+  const int M = reg_iterations(pinv_cutoff);
+  double* part = reinterpret_cast<double*>(workspace);
+  double* scal = part + (size_t)(M > 0 ? M : 1) * chunks;
+  cudaStream_t st = as_stream(stream);
+  const double2* v2 = reinterpret_cast<const double2*>(vtf);
+  if (M > 0) {
+    tdvp_reg_partial_kernel<<<dim3(chunks, M), 256, 0, st>>>(ev, v2, snr, n, pinv_cutoff, snr_tol, part, chunks);
+    int rc = check_launch("vmc_tdvp_regularize(partial)");
+    if (rc) return rc;
+  }
+  tdvp_reg_select_kernel<<<1, 1024, 0, st>>>(v2, n, part, chunks, M, pinv_cutoff, pinv_tol, result, scal);
+  int rc = check_launch("vmc_tdvp_regularize(select)");
+  if (rc) return rc;
+  tdvp_reg_write_kernel<<<(n + 255) / 256, 256, 0, st>>>(ev, snr, n, snr_tol, scal, pinv);
   return check_launch("vmc_tdvp_regularize");
 }
 

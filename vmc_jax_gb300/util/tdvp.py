@@ -196,8 +196,10 @@ class TDVP:
         pinv = torch.empty(P, dtype=torch.float64, device=dev)
         res = torch.empty(3, dtype=torch.float64, device=dev)
         useSnr = not isinstance(self.sampler, ExactSampler)
+        ws = _lib.Workspace.get(_lib.query("vmc_tdvp_regularize_workspace_bytes", P, float(self.pinvCutoff)))
         _lib.call("vmc_tdvp_regularize", _lib.ptr(ev), _lib.ptr(vtf), _lib.ptr(snr) if useSnr else None, P,
-                  float(self.pinvCutoff), float(self.pinvTol), float(self.snrTol), _lib.ptr(pinv), _lib.ptr(res), st)
+                  float(self.pinvCutoff), float(self.pinvTol), float(self.snrTol), _lib.ptr(pinv), _lib.ptr(res),
+                  _lib.ptr(ws), ws.numel(), st)
         coef = (pinv.to(torch.complex128) * vtf).contiguous()
         z = torch.empty(P, dtype=torch.complex128, device=dev)
         ws = _lib.Workspace.get(_lib.query("vmc_zgemv_workspace_bytes", P))
