@@ -63,6 +63,7 @@ struct data_args {
   const double2* force;    // (P) f_k = -x * covar(O,E)_k (SNR data) or null
   int format;
   int tileN;  // samples per block
+  int colChunk;  // columns per block (grid y)
   int64_t ld; // leading dimension of the output (elements)
   void* out;
   void* out2;              // lo plane for BF16X2
@@ -126,6 +127,7 @@ __global__ void __launch_bounds__(256) rbm_data_kernel(const int32_t* __restrict
   const int64_t n0 = (int64_t)blockIdx.x * kTileN;
   tile_tanh<T>(configs, n0, a.N, a.L, a.M, W, b, tt, sg, kTileN);
   const int P = a.M * a.L + (a.hasBias ? a.M : 0);
+  const int k0 = blockIdx.y * a.colChunk, k1 = min(P, k0 + a.colChunk);
   const int tid = threadIdx.x;
   if (a.format == VMC_DATA_BF16X2 && a.eloc == nullptr) {
     // transposed planes (2P, N): thread -> (sample lane r, column group)
@@ -137,8 +139,8 @@ __global__ void __launch_bounds__(256) rbm_data_kernel(const int32_t* __restrict
     if (n < a.N) {
       const double sw = sqrt(a.w[n]);
       col_pos c;
-      c.set(cg, a.M, a.hasBias);
-      for (int k = cg; k < P; k += ncg, c.advance(ncg, a.M)) {
+      c.set(k0 + cg, a.M, a.hasBias);
+      for (int k = k0 + cg; k < k1; k += ncg, c.advance(ncg, a.M)) {
         cpx<double> v = data_value<T>(a, tt, sg, r, n, k, c, sw);
         float vr = (float)v.re, vi = (float)v.im;
         __nv_bfloat16 hr = __float2bfloat16_rn(vr), hi_ = __float2bfloat16_rn(vi);
@@ -156,8 +158,8 @@ __global__ void __launch_bounds__(256) rbm_data_kernel(const int32_t* __restrict
     if (n >= a.N) break;
     const double sw = sqrt(a.w[n]);
     col_pos c;
-    c.set(tid, a.M, a.hasBias);
-    for (int k = tid; k < P; k += blockDim.x, c.advance(blockDim.x, a.M)) {
+    c.set(k0 + tid, a.M, a.hasBias);
+    for (int k = k0 + tid; k < k1; k += blockDim.x, c.advance(blockDim.x, a.M)) {
       cpx<double> v = data_value<T>(a, tt, sg, r, n, k, c, sw);
       if (a.format == VMC_DATA_C128) {
         reinterpret_cast<double2*>(a.out)[n * a.ld + k] = make_double2(v.re, v.im);
@@ -201,7 +203,13 @@ static int launch_data(int32_t precision, const int32_t* configs, const void* ke
   a.tileN = kTileN;
   const size_t smem = (size_t)kTileN * a.M * el + (size_t)kTileN * a.L;
   VMC_REQUIRE(smem <= 227 * 1024, VMC_ERR_UNSUPPORTED, "%s: M=%d, L=%d too large for one tile", fn, a.M, a.L);
-  const int grid = (int)((a.N + kTileN - 1) / kTileN);
+  // columns split over grid y so that enough blocks are resident; each block
+  // recomputes tanh(theta) of its samples (L M per sample, small next to the
+  // column loop)
+  const int64_t P = (int64_t)a.M * a.L + (a.hasBias ? a.M : 0);
+  a.colChunk = 2048;
+  const dim3 grid((unsigned)((a.N + kTileN - 1) / kTileN), (unsigned)((P + a.colChunk - 1) / a.colChunk));
+  VMC_REQUIRE(grid.y <= 65535, VMC_ERR_UNSUPPORTED, "%s: %lld columns", fn, (long long)P);
   cudaStream_t st = as_stream(stream);
   if (precision == VMC_F64) {
     if (smem > 48 * 1024)
