@@ -26,7 +26,7 @@ __device__ void tile_tanh(const int32_t* __restrict__ configs, int64_t n0, int64
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
   for (int r = warp; r < kTileN; r += nwarps) {
     const int64_t n = n0 + r;
-    int8_t* cfg = sg + r * L;
+    int8_t* cfg = sg + r * (L + 1);
     if (n < N) {
       for (int i = lane; i < L; i += 32) cfg[i] = (int8_t)configs[n * L + i];
     } else {
@@ -45,7 +45,7 @@ __device__ void tile_tanh(const int32_t* __restrict__ configs, int64_t n0, int64
           th.im -= x.im;
         }
       }
-      tt[(size_t)r * M + j] = n < N ? ctanh_(th) : mk(T(0), T(0));
+      tt[(size_t)r * (M + 1) + j] = n < N ? ctanh_(th) : mk(T(0), T(0));
     }
   }
   __syncthreads();
@@ -103,8 +103,8 @@ struct col_pos {
 template <typename T>
 __device__ __forceinline__ cpx<double> data_value(const data_args& a, const cpx<T>* tt, const int8_t* sg, int r,
                                                   int64_t n, int k, const col_pos& c, double sw) {
-  cpx<T> o = tt[(size_t)r * a.M + c.j];
-  if (!c.bias && !sg[r * a.L + c.i]) o = mk(-o.re, -o.im);
+  cpx<T> o = tt[(size_t)r * (a.M + 1) + c.j];
+  if (!c.bias && !sg[r * (a.L + 1) + c.i]) o = mk(-o.re, -o.im);
   const double2 mu = a.okMean[k];
   cpx<double> d = mk((double)o.re - mu.x, (double)o.im - mu.y);
   if (a.eloc) {
@@ -123,7 +123,9 @@ __global__ void __launch_bounds__(256) rbm_data_kernel(const int32_t* __restrict
   extern __shared__ unsigned char smem[];
   const int kTileN = a.tileN;
   cpx<T>* tt = reinterpret_cast<cpx<T>*>(smem);
-  int8_t* sg = reinterpret_cast<int8_t*>(smem + (size_t)kTileN * a.M * sizeof(cpx<T>));
+  // rows padded by one element: lanes of the transposed store loop read
+  // different rows, which would otherwise fall into the same bank
+  int8_t* sg = reinterpret_cast<int8_t*>(smem + (size_t)kTileN * (a.M + 1) * sizeof(cpx<T>));
   const int64_t n0 = (int64_t)blockIdx.x * kTileN;
   tile_tanh<T>(configs, n0, a.N, a.L, a.M, W, b, tt, sg, kTileN);
   const int P = a.M * a.L + (a.hasBias ? a.M : 0);
@@ -199,15 +201,15 @@ static int launch_data(int32_t precision, const int32_t* configs, const void* ke
   }
   const size_t el = precision == VMC_F64 ? 16 : 8;
   int kTileN = 64;
-  while (kTileN > 8 && (size_t)kTileN * (a.M * el + a.L) > 200 * 1024) kTileN /= 2;
+  while (kTileN > 8 && (size_t)kTileN * ((a.M + 1) * el + a.L + 1) > 200 * 1024) kTileN /= 2;
   a.tileN = kTileN;
-  const size_t smem = (size_t)kTileN * a.M * el + (size_t)kTileN * a.L;
+  const size_t smem = (size_t)kTileN * (a.M + 1) * el + (size_t)kTileN * (a.L + 1);
   VMC_REQUIRE(smem <= 227 * 1024, VMC_ERR_UNSUPPORTED, "%s: M=%d, L=%d too large for one tile", fn, a.M, a.L);
   // columns split over grid y so that enough blocks are resident; each block
   // recomputes tanh(theta) of its samples (L M per sample, small next to the
   // column loop)
   const int64_t P = (int64_t)a.M * a.L + (a.hasBias ? a.M : 0);
-  a.colChunk = 2048;
+  a.colChunk = 4096;
   const dim3 grid((unsigned)((a.N + kTileN - 1) / kTileN), (unsigned)((P + a.colChunk - 1) / a.colChunk));
   VMC_REQUIRE(grid.y <= 65535, VMC_ERR_UNSUPPORTED, "%s: %lld columns", fn, (long long)P);
   cudaStream_t st = as_stream(stream);
