@@ -117,20 +117,69 @@ __device__ __forceinline__ cpx<double> data_value(const data_args& a, const cpx<
   return mk(sw * d.re, sw * d.im);
 }
 
+// The same value in FP32 for the BF16 hi/lo and complex64 formats, from
+// per-block staged column means / forces and per-sample sqrt(w) and
+// (-x)(E_n - Ebar): their precision is far below FP32's, and GB300's FP64
+// rate would otherwise bound this HBM-streaming kernel.
+template <typename T>
+__device__ __forceinline__ cpx<float> data_value_f(const data_args& a, const cpx<T>* tt, const int8_t* sg, int r,
+                                                  const col_pos& c, float2 mu, float2 f, float sw, float2 xde) {
+  cpx<T> o = tt[(size_t)r * (a.M + 1) + c.j];
+  if (!c.bias && !sg[r * (a.L + 1) + c.i]) o = mk(-o.re, -o.im);
+  cpx<float> d = mk((float)o.re - mu.x, (float)o.im - mu.y);
+  if (a.eloc) {
+    const cpx<float> h = mk(xde.x, xde.y) * conjg(d);
+    d = mk(h.re - f.x, h.im - f.y);
+  }
+  return mk(sw * d.re, sw * d.im);
+}
+
+__device__ __forceinline__ void store_split(__nv_bfloat16* hi, __nv_bfloat16* lo, size_t idx, float v) {
+  const __nv_bfloat16 h = __float2bfloat16_rn(v);
+  hi[idx] = h;
+  lo[idx] = __float2bfloat16_rn(v - __bfloat162float(h));
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) rbm_data_kernel(const int32_t* __restrict__ configs, const cpx<T>* __restrict__ W,
                                                        const cpx<T>* __restrict__ b, data_args a) {
-  extern __shared__ unsigned char smem[];
+  extern __shared__ __align__(16) unsigned char smem[];
   const int kTileN = a.tileN;
   cpx<T>* tt = reinterpret_cast<cpx<T>*>(smem);
   // rows padded by one element: lanes of the transposed store loop read
   // different rows, which would otherwise fall into the same bank
   int8_t* sg = reinterpret_cast<int8_t*>(smem + (size_t)kTileN * (a.M + 1) * sizeof(cpx<T>));
+  const size_t stOff = ((size_t)kTileN * (a.M + 1) * sizeof(cpx<T>) + (size_t)kTileN * (a.L + 1) + 15) & ~(size_t)15;
+  float2* cmean = reinterpret_cast<float2*>(smem + stOff);
+  float2* cforce = cmean + a.colChunk;
+  float2* sxde = cforce + a.colChunk;
+  float* ssw = reinterpret_cast<float*>(sxde + kTileN);
   const int64_t n0 = (int64_t)blockIdx.x * kTileN;
-  tile_tanh<T>(configs, n0, a.N, a.L, a.M, W, b, tt, sg, kTileN);
   const int P = a.M * a.L + (a.hasBias ? a.M : 0);
   const int k0 = blockIdx.y * a.colChunk, k1 = min(P, k0 + a.colChunk);
   const int tid = threadIdx.x;
+  const bool lowp = a.format != VMC_DATA_C128;
+  if (lowp) {
+    for (int k = k0 + tid; k < k1; k += blockDim.x) {
+      const double2 mu = a.okMean[k];
+      cmean[k - k0] = make_float2((float)mu.x, (float)mu.y);
+      if (a.eloc) {
+        const double2 f = a.force[k];
+        cforce[k - k0] = make_float2((float)f.x, (float)f.y);
+      }
+    }
+    for (int r = tid; r < kTileN; r += blockDim.x) {
+      const int64_t n = n0 + r;
+      ssw[r] = n < a.N ? (float)sqrt(a.w[n]) : 0.f;
+      if (a.eloc && n < a.N) {
+        const double2 e = a.eloc[n], em = *a.elocMean;
+        const cpx<double> xde = mk(a.xfac.x, a.xfac.y) * mk(e.x - em.x, e.y - em.y);
+        sxde[r] = make_float2((float)xde.re, (float)xde.im);
+      }
+    }
+  }
+  tile_tanh<T>(configs, n0, a.N, a.L, a.M, W, b, tt, sg, kTileN);  // ends with __syncthreads
+  const float2 zero2 = make_float2(0.f, 0.f);
   if (a.format == VMC_DATA_BF16X2 && a.eloc == nullptr) {
     // transposed planes (2P, N): thread -> (sample lane r, column group)
     __nv_bfloat16* hi = reinterpret_cast<__nv_bfloat16*>(a.out);
@@ -139,17 +188,13 @@ __global__ void __launch_bounds__(256) rbm_data_kernel(const int32_t* __restrict
     const int cg = tid / kTileN, ncg = blockDim.x / kTileN;
     const int64_t n = n0 + r;
     if (n < a.N) {
-      const double sw = sqrt(a.w[n]);
+      const float sw = ssw[r];
       col_pos c;
       c.set(k0 + cg, a.M, a.hasBias);
       for (int k = k0 + cg; k < k1; k += ncg, c.advance(ncg, a.M)) {
-        cpx<double> v = data_value<T>(a, tt, sg, r, n, k, c, sw);
-        float vr = (float)v.re, vi = (float)v.im;
-        __nv_bfloat16 hr = __float2bfloat16_rn(vr), hi_ = __float2bfloat16_rn(vi);
-        hi[(size_t)k * a.ld + n] = hr;
-        lo[(size_t)k * a.ld + n] = __float2bfloat16_rn(vr - __bfloat162float(hr));
-        hi[(size_t)(P + k) * a.ld + n] = hi_;
-        lo[(size_t)(P + k) * a.ld + n] = __float2bfloat16_rn(vi - __bfloat162float(hi_));
+        const cpx<float> v = data_value_f<T>(a, tt, sg, r, c, cmean[k - k0], zero2, sw, zero2);
+        store_split(hi, lo, (size_t)k * a.ld + n, v.re);
+        store_split(hi, lo, (size_t)(P + k) * a.ld + n, v.im);
       }
     }
     return;
@@ -158,24 +203,28 @@ __global__ void __launch_bounds__(256) rbm_data_kernel(const int32_t* __restrict
   for (int r = 0; r < kTileN; ++r) {
     const int64_t n = n0 + r;
     if (n >= a.N) break;
-    const double sw = sqrt(a.w[n]);
     col_pos c;
     c.set(k0 + tid, a.M, a.hasBias);
-    for (int k = k0 + tid; k < k1; k += blockDim.x, c.advance(blockDim.x, a.M)) {
-      cpx<double> v = data_value<T>(a, tt, sg, r, n, k, c, sw);
-      if (a.format == VMC_DATA_C128) {
+    if (!lowp) {
+      const double sw = sqrt(a.w[n]);
+      for (int k = k0 + tid; k < k1; k += blockDim.x, c.advance(blockDim.x, a.M)) {
+        const cpx<double> v = data_value<T>(a, tt, sg, r, n, k, c, sw);
         reinterpret_cast<double2*>(a.out)[n * a.ld + k] = make_double2(v.re, v.im);
-      } else if (a.format == VMC_DATA_C64) {
-        reinterpret_cast<float2*>(a.out)[n * a.ld + k] = make_float2((float)v.re, (float)v.im);
+      }
+      continue;
+    }
+    const float sw = ssw[r];
+    const float2 xde = a.eloc ? sxde[r] : zero2;
+    for (int k = k0 + tid; k < k1; k += blockDim.x, c.advance(blockDim.x, a.M)) {
+      const cpx<float> v =
+          data_value_f<T>(a, tt, sg, r, c, cmean[k - k0], a.eloc ? cforce[k - k0] : zero2, sw, xde);
+      if (a.format == VMC_DATA_C64) {
+        reinterpret_cast<float2*>(a.out)[n * a.ld + k] = make_float2(v.re, v.im);
       } else {  // BF16X2 row-major (N, 2P)
         __nv_bfloat16* hi = reinterpret_cast<__nv_bfloat16*>(a.out);
         __nv_bfloat16* lo = reinterpret_cast<__nv_bfloat16*>(a.out2);
-        float vr = (float)v.re, vi = (float)v.im;
-        __nv_bfloat16 hr = __float2bfloat16_rn(vr), hi_ = __float2bfloat16_rn(vi);
-        hi[n * a.ld + k] = hr;
-        lo[n * a.ld + k] = __float2bfloat16_rn(vr - __bfloat162float(hr));
-        hi[n * a.ld + P + k] = hi_;
-        lo[n * a.ld + P + k] = __float2bfloat16_rn(vi - __bfloat162float(hi_));
+        store_split(hi, lo, n * a.ld + k, v.re);
+        store_split(hi, lo, n * a.ld + P + k, v.im);
       }
     }
   }
@@ -201,15 +250,16 @@ static int launch_data(int32_t precision, const int32_t* configs, const void* ke
   }
   const size_t el = precision == VMC_F64 ? 16 : 8;
   int kTileN = 64;
-  while (kTileN > 8 && (size_t)kTileN * ((a.M + 1) * el + a.L + 1) > 200 * 1024) kTileN /= 2;
+  while (kTileN > 8 && (size_t)kTileN * ((a.M + 1) * el + a.L + 1) > 180 * 1024) kTileN /= 2;
   a.tileN = kTileN;
-  const size_t smem = (size_t)kTileN * (a.M + 1) * el + (size_t)kTileN * (a.L + 1);
+  a.colChunk = 2048;
+  const size_t tileBytes = ((size_t)kTileN * (a.M + 1) * el + (size_t)kTileN * (a.L + 1) + 15) & ~(size_t)15;
+  const size_t smem = tileBytes + (size_t)a.colChunk * 16 + (size_t)kTileN * 12;
   VMC_REQUIRE(smem <= 227 * 1024, VMC_ERR_UNSUPPORTED, "%s: M=%d, L=%d too large for one tile", fn, a.M, a.L);
   // columns split over grid y so that enough blocks are resident; each block
   // recomputes tanh(theta) of its samples (L M per sample, small next to the
   // column loop)
   const int64_t P = (int64_t)a.M * a.L + (a.hasBias ? a.M : 0);
-  a.colChunk = 4096;
   const dim3 grid((unsigned)((a.N + kTileN - 1) / kTileN), (unsigned)((P + a.colChunk - 1) / a.colChunk));
   VMC_REQUIRE(grid.y <= 65535, VMC_ERR_UNSUPPORTED, "%s: %lld columns", fn, (long long)P);
   cudaStream_t st = as_stream(stream);
