@@ -661,6 +661,7 @@ def main():
     clocks = ClockSampler(local)
     TIMER.reset()
     TIMER.enabled = True
+    TIMER.nvtx = True
     V._lib.launch_count = 0
     barrier()
     torch.cuda.synchronize()
@@ -675,6 +676,8 @@ def main():
     barrier()
     clock = clocks.stop()
     TIMER.enabled = False
+    TIMER.nvtx = False
+    TIMER.close()
     launches = V._lib.launch_count
     ms = reduce_max_ms(t_start.elapsed_time(t_end), device=torch.device("cuda", local))
     ms_per_step = ms / args.steps

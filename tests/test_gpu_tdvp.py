@@ -180,3 +180,38 @@ def test_minsr_update_matches_oracle(cuda):
     uo = O.MinSR(eso, pinvTol=1e-8)(opsi.get_parameters(), 0., psi=opsi, hamiltonian=O.tfim(8, 1.0, 0.9),
                                     intStep=0)
     assert _rel(u.cpu().numpy(), uo) < 1e-8
+
+
+def test_checkpoint_resume_reproduces_the_run(cuda, tmp_path):
+    """save_checkpoint after two steps; the resumed run (fresh objects) makes
+    the same next two steps as the uninterrupted one, bit for bit (chains and
+    random-stream position restored)."""
+    import vmc_jax_gb300 as V
+
+    def make():
+        psi, _ = _pair(8, 6, True, 0.2, seed=31)
+        mc = V.sampler.MCSampler(psi, (8,), 5, updateProposer=V.sampler.propose_spin_flip, numChains=32,
+                                 numSamples=512, thermalizationSweeps=2, sweepSteps=8)
+        td = V.util.TDVP(mc, makeReal="real", rhsPrefactor=1., pinvCutoff=1e-8, snrTol=2)
+        return psi, mc, td, V.util.stepper.AdaptiveHeun(timeStep=1e-3, tol=1e-3)
+
+    H = _tfim(V, 8, 1.0, 0.7)
+
+    def steps(psi, td, st, n):
+        out = []
+        for _ in range(n):
+            th, dt = st.step(0, td, psi.get_parameters(), hamiltonian=H, psi=psi, numSamples=512)
+            psi.set_parameters(th)
+            out.append(th.cpu().numpy())
+        return out
+
+    psi, mc, td, st = make()
+    steps(psi, td, st, 2)
+    path = str(tmp_path / "ckpt.pt")
+    V.util.save_checkpoint(path, psi, mc, st, t=0.5)
+    ref = steps(psi, td, st, 2)
+    psi2, mc2, td2, st2 = make()
+    assert V.util.load_checkpoint(path, psi2, mc2, st2) == 0.5
+    got = steps(psi2, td2, st2, 2)
+    for a, b in zip(got, ref):
+        assert np.array_equal(a, b)

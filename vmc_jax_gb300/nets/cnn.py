@@ -102,8 +102,9 @@ class CNN:
         shape = sampleShape if sampleShape is not None else self._shape
         out = torch.empty(N, dtype=torch.complex128, device=configs.device)
         d = self.desc(shape)
+        theta = self.flat(params, precision)  # kept alive until the launch is enqueued
         _lib.call("vmc_cnn_logpsi", self._prec(precision), _lib.ctypes_ref(d), _lib.ptr(configs), N,
-                  _lib.ptr(self.flat(params, precision)), _lib.ptr(out), _lib.stream())
+                  _lib.ptr(theta), _lib.ptr(out), _lib.stream())
         return out
 
     def gradients(self, params, configs, precision="fp64", layout=_lib.VMC_GRAD_REFERENCE, sampleShape=None):
@@ -115,8 +116,9 @@ class CNN:
             out = torch.empty((N, P), dtype=torch.complex128, device=configs.device)
         else:
             out = torch.empty((N, P), dtype=torch.float64, device=configs.device)
+        theta = self.flat(params, precision)
         _lib.call("vmc_cnn_gradients", self._prec(precision), _lib.ctypes_ref(d), _lib.ptr(configs), N,
-                  _lib.ptr(self.flat(params, precision)), layout, _lib.ptr(out), _lib.stream())
+                  _lib.ptr(theta), layout, _lib.ptr(out), _lib.stream())
         return out
 
 

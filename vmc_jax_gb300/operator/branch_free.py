@@ -316,8 +316,9 @@ class BranchFreeOperator(Operator):
         from ..nets.cnn import CNN
         if isinstance(psi.net, CNN):
             d = psi.net.desc(tuple(s.shape[2:]))
-            _lib.call("vmc_cnn_oloc_fused", prec, _lib.ctypes_ref(d), _lib.ptr(flat), N,
-                      _lib.ptr(psi.net.flat(params, psi.precision)), op, _lib.ptr(lps), _lib.ptr(out), _lib.stream())
+            theta = psi.net.flat(params, psi.precision)  # kept alive until the launch is enqueued
+            _lib.call("vmc_cnn_oloc_fused", prec, _lib.ctypes_ref(d), _lib.ptr(flat), N, _lib.ptr(theta), op,
+                      _lib.ptr(lps), _lib.ptr(out), _lib.stream())
             return out.reshape(s.shape[:2])
         M = int(params["kernel"].shape[1])
         from ..nets.sym_wrapper import SymNet

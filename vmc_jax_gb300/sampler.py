@@ -134,8 +134,9 @@ class MCSampler:
             out = torch.empty((perChain * C, self.L), dtype=torch.int32, device=self.states.device)
             self.counters.zero_()
             d = psi.net.desc(self.sampleShape)
+            theta = psi.net.flat(params, psi.precision)  # kept alive until the launch is enqueued
             _lib.call("vmc_cnn_metropolis", prec, _lib.ctypes_ref(d), _lib.ptr(self.states), C,
-                      _lib.ptr(psi.net.flat(params, psi.precision)), float(self.mu), self.seed,
+                      _lib.ptr(theta), float(self.mu), self.seed,
                       self.callIndex & 0xFFFFFFFF, int(self.thermalizationSweeps * self.sweepSteps),
                       int(self.sweepSteps), int(perChain), _lib.ptr(out), _lib.ptr(self.counters), _lib.stream())
             self.callIndex += 1

@@ -17,10 +17,16 @@ x = 1) or a real-time quench (makeReal='imag', x = i), Euler-integrated.
   whichever jobs are ready again.
 * Per-step latency (graph launch to update applied) and per-job latency
   (arrival to last step) are recorded for p50/p99 reporting.
+* Failures stay with their job: an invalid spec is refused at ``submit``, a
+  job whose footprint exceeds the whole budget is rejected at admission, a
+  job whose step raises (including its ``on_step`` callback) is marked
+  failed, and ``cancel`` withdraws a queued job or stops an active one after
+  its current step; the other jobs continue.  ``status`` reports each job's
+  state.
 
 A job computes exactly what it computes alone: its kernels, inputs and
-random stream do not depend on the other jobs; only the FP32 atomic column
-sums of the SNR contraction can round differently run to run.
+random stream do not depend on the other jobs, and every reduction adds in
+a fixed order.
 """
 
 import dataclasses
@@ -55,6 +61,15 @@ class JobSpec:
     chains: int = 0              # 0: min(1024, num_samples // 4)
     precision: str = "mixed"
     arrival: float = 0.0         # seconds after the server starts
+    on_step: object = None       # callable(job_id, step, energy) after every step
+
+    def validate(self):
+        if self.L < 2 or self.M < 1 or self.num_samples < 1 or self.steps < 0:
+            raise ValueError("job spec needs L >= 2, M >= 1, num_samples >= 1, steps >= 0")
+        if self.kind not in ("ground_state", "quench"):
+            raise ValueError("job kind must be 'ground_state' or 'quench', not %r" % (self.kind,))
+        if self.precision not in ("fp64", "fp32", "mixed"):
+            raise ValueError("precision must be 'fp64', 'fp32' or 'mixed'")
 
     @property
     def num_params(self):
@@ -173,6 +188,8 @@ class _Slot:
             self.stream.synchronize()
         self.steps_done += 1
         self.step_latencies.append(time.perf_counter() - t_launch)
+        if self.spec.on_step is not None:
+            self.spec.on_step(self.id, self.steps_done, float(self.energies[-1]))
 
     @property
     def finished(self):
@@ -205,14 +222,35 @@ class Server:
         self.sample_stream = torch.cuda.Stream()
         self.max_resident = 0
         self.graph_launches = 0
+        self.states = {}        # job id -> queued / active / done / failed / rejected / cancelled
+        self.errors = {}
+        self.cancelled = set()
 
     def submit(self, spec):
+        """Queue a job; raises ValueError for an invalid spec."""
+        spec.validate()
         with self.lock:
             jid = self.next_id
             self.next_id += 1
             self.queue.append((jid, spec))
+            self.states[jid] = "queued"
             self.lock.notify_all()
             return jid
+
+    def cancel(self, job_id):
+        """Withdraw a queued job, or stop an active one after its current step."""
+        with self.lock:
+            for item in list(self.queue):
+                if item[0] == job_id:
+                    self.queue.remove(item)
+                    self.states[job_id] = "cancelled"
+                    self.lock.notify_all()
+                    return
+            if job_id in self.active:
+                self.cancelled.add(job_id)
+
+    def status(self, job_id):
+        return self.states.get(job_id)
 
     def _used(self):
         return sum(footprint_bytes(s.spec) for s in self.active.values())
@@ -225,14 +263,23 @@ class Server:
                 continue
             if len(self.active) >= self.max_slots:
                 break
+            if footprint_bytes(spec) > self.hbm_budget:
+                self.queue.remove(item)
+                self.states[jid] = "rejected"
+                self.errors[jid] = "needs %.1f GB, more than the HBM budget of %.1f GB" % (
+                    footprint_bytes(spec) / 1e9, self.hbm_budget / 1e9)
+                continue
             if self._used() + footprint_bytes(spec) > self.hbm_budget:
-                if not self.active:
-                    raise RuntimeError("job %d needs %.1f GB, more than the HBM budget"
-                                       % (jid, footprint_bytes(spec) / 1e9))
                 continue
             self.queue.remove(item)
-            slot = _Slot(jid, spec, self.t0 + spec.arrival)
+            try:
+                slot = _Slot(jid, spec, self.t0 + spec.arrival)
+            except Exception as e:  # e.g. device memory exhausted while allocating the slot
+                self.states[jid] = "failed"
+                self.errors[jid] = "admission: %s" % (e,)
+                continue
             self.active[jid] = slot
+            self.states[jid] = "active"
             self.ready.add(jid)
             admitted.append(jid)
         self.max_resident = max(self.max_resident, len(self.active))
@@ -279,7 +326,13 @@ class Server:
             with self.lock:
                 ids = sorted(self.ready)
                 self.ready.clear()
+                for jid in [i for i in ids if i in self.cancelled]:  # cancelled between steps
+                    del self.active[jid]
+                    self.states[jid] = "cancelled"
+                ids = [i for i in ids if i not in self.cancelled]
                 self.graphs = {k: v for k, v in self.graphs.items() if all(i in self.active for i in k)}
+                if not ids:
+                    continue
             g = self._graph_for(ids)
             t_launch = time.perf_counter()
             with torch.cuda.stream(self.sample_stream):
@@ -297,12 +350,23 @@ class Server:
         return self.report()
 
     def _work(self, slot, ev, t_launch):
-        slot.solve(ev, t_launch)
+        err = None
+        try:
+            slot.solve(ev, t_launch)
+        except Exception as e:  # the job fails alone; its slot is released
+            err = "%s: %s" % (type(e).__name__, e)
         with self.lock:
-            if slot.finished:
+            if err is not None or slot.id in self.cancelled or slot.finished:
                 slot.job_latency = time.perf_counter() - slot.arrival_wall
-                self.done[slot.id] = slot
                 del self.active[slot.id]
+                if err is not None:
+                    self.states[slot.id] = "failed"
+                    self.errors[slot.id] = err
+                elif slot.finished:
+                    self.done[slot.id] = slot
+                    self.states[slot.id] = "done"
+                else:
+                    self.states[slot.id] = "cancelled"
             else:
                 self.ready.add(slot.id)
             self.lock.notify_all()
@@ -315,9 +379,13 @@ class Server:
                 "steps_per_s": len(steps) / wall if wall > 0 else None,
                 "step_latency_s": {"p50": percentile(steps, 50), "p99": percentile(steps, 99)},
                 "job_latency_s": {"p50": percentile(jobs, 50), "p99": percentile(jobs, 99)},
-                "max_resident_jobs": self.max_resident, "graph_launches": self.graph_launches}
+                "max_resident_jobs": self.max_resident, "graph_launches": self.graph_launches,
+                "not_completed": {jid: st for jid, st in self.states.items() if st != "done"}}
 
     def result(self, job_id):
         """Final flat parameters and per-step energies of a finished job."""
+        if job_id not in self.done:
+            raise KeyError("job %d is %s%s" % (job_id, self.states.get(job_id, "unknown"),
+                                               (": " + self.errors[job_id]) if job_id in self.errors else ""))
         s = self.done[job_id]
         return s.theta, torch.stack(s.energies)
