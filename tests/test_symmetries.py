@@ -51,3 +51,43 @@ def test_orbit_codes_reject_non_permutations():
     o[0, 0, 0] = o[0, 1, 0] = o[0, 2, 2] = 1
     with pytest.raises(ValueError):
         S.orbit_codes(o)
+
+
+def test_oracle_symnet_sector_signs():
+    """symmetries_test.py:46-85 on the oracle: in the odd sector of a
+    reflection / translation / spin flip, psi(g s) = -psi(s)."""
+    L = 10
+    rng = np.random.default_rng(0)
+    prm = O.init_cpx_rbm(L, 2, True, rng, scale=0.3)
+    c1 = rng.permutation(np.array([0, 1] * (L // 2)))
+    for use, c2 in (("reflection", c1[::-1]), ("translation", np.roll(c1, 1)), ("spinflip", 1 - c1)):
+        o, f = O.get_orbit_1D(L, use, reflection_factor=-1., translation_factor=np.exp(1j * np.pi),
+                              spinflip_factor=-1.)
+        net = O.SymNet(O.CpxRBM(2, True), o, f)
+        a = net.apply(prm, c1[None])[0]
+        b = net.apply(prm, c2[None].copy())[0]
+        assert abs(1 + np.exp(a - b)) < 1e-10
+
+
+def test_oracle_symnet_gradient_finite_difference():
+    """The oracle's SymNet gradient (weights f exp(lp_tau - lp)) against
+    central differences of its log psi (vqs_test.py:104-125)."""
+    L = 6
+    rng = np.random.default_rng(1)
+    prm = O.init_cpx_rbm(L, 3, True, rng, scale=0.3)
+    o, f = O.get_orbit_1D(L, "translation", "reflection", translation_factor=np.exp(0.4j))
+    for avg in (O.avgFun_Coefficients_Exp, O.avgFun_Coefficients_Log):
+        psi = O.NQS(O.SymNet(O.CpxRBM(3, True), o, f, avg), prm)
+        s = rng.integers(0, 2, (1, 5, L))
+        G = psi.gradients(s)[0]
+        th = psi.get_parameters()
+        eps = 1e-6
+        for j in range(0, th.size, 7):
+            u = np.zeros(th.size)
+            u[j] = eps
+            psi.set_parameters(th + u)
+            up = psi(s)[0]
+            psi.set_parameters(th - u)
+            dn = psi(s)[0]
+            psi.set_parameters(th)
+            assert np.max(np.abs((up - dn) / (2 * eps) - G[:, j])) < 1e-6
