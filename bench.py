@@ -355,7 +355,9 @@ def run_reference(args):
         import threadpoolctl  # noqa: F401
     except Exception:
         pass
-    for _ in range(args.warmup):
+    # one warm-up sample loads BLAS thread pools and pages; further ones only
+    # lengthen the run (the CPU path has nothing to compile)
+    for _ in range(min(args.warmup, 1)):
         cpu_step_seconds(cfg, "")
     secs = []
     for _ in range(args.steps):
@@ -366,7 +368,7 @@ def run_reference(args):
     emit({"metric": "TDVP steps/s", "value": val, "unit": "steps/s", "n_gpus": args.gpus, "steps": args.steps,
           "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak",
           "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "impl": "reference",
-          "config": {"workload": args.workload, **cfg},
+          "config": {"workload": args.workload, **cfg}, "warmup_samples_run": min(args.warmup, 1),
           "cpu_baseline": {"value": val, "unit": "steps/s", "cores": os.cpu_count(), "kind": "port",
                            "sample": cpu_sample_desc(cfg)},
           "e2e": {"value": val, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
