@@ -646,7 +646,9 @@ extern "C" int vmc_rbm_grad_stats(int32_t precision, const int32_t* configs, int
 // registers.  A proposal flips one site i (propose_spin_flip,
 // sampler.py:15-19) and is accepted iff u < |psi(s')/psi(s)|^mu with
 //   |psi(s')/psi(s)|^2 = prod_j |cosh(2W_ij) - sigma_i tanh(theta_j) sinh(2W_ij)|^2
-// (no network re-evaluation).  On acceptance theta_j -= 2 sigma_i W_ij.
+// (no network re-evaluation), evaluated as |prod_j cosh 2W_ij|^2
+// prod_j |1 - sigma_i tanh(theta_j) tanh(2W_ij)|^2 from the tanh(2W) table
+// and the row sums of log cosh 2W.  On acceptance theta_j -= 2 sigma_i W_ij.
 // Site and u come from the Philox stream metropolis_draw(seed, call, step,
 // chain); steps are numbered from 0 within one call.
 // ===================================================================
@@ -690,41 +692,44 @@ __global__ void __launch_bounds__(256) rbm_metropolis_kernel(
     tn[q] = ctanh_(t);
   }
   const size_t LM = (size_t)L * M;
-  const cpx<T>* tC = tab;
-  const cpx<T>* tS = tab + LM;
+  // cosh(theta + D)/cosh(theta) = cosh 2W (1 - s tanh(theta) tanh 2W): one
+  // tanh(2W) row per proposal, the row's |prod_j cosh 2W|^2 =
+  // exp(2 Re rowLogC) added to the log-ratio
+  const cpx<T>* tT = tab + 4 * LM;
+  const cpx<T>* rowLogC = tab + 5 * LM;
   const T halfMu = T(0.5 * mu);
   unsigned long long accepted = 0;
   const int64_t total = thermSteps + sweepSteps * samplesPerChain;
   // the flip site does not depend on the chain state: the next step's table
-  // rows are loaded while the current step is evaluated
+  // row is loaded while the current step is evaluated
   mc_draw d = metropolis_draw(seed, call, 0u, (uint32_t)chain, L);
-  cpx<T> fC[JPL], fS[JPL];
+  cpx<T> fT[JPL];
+  T rowRe = rowLogC[d.site].re;
 #pragma unroll
   for (int q = 0; q < JPL; ++q) {
     const int j = lane + 32 * q;
-    fC[q] = j < M ? tC[(size_t)d.site * M + j] : mk(T(1), T(0));
-    fS[q] = j < M ? tS[(size_t)d.site * M + j] : mk(T(0), T(0));
+    fT[q] = j < M ? tT[(size_t)d.site * M + j] : mk(T(0), T(0));
   }
   for (int64_t step = 0; step < total; ++step) {
     const int i = d.site;
     const mc_draw dn = metropolis_draw(seed, call, (uint32_t)(step + 1), (uint32_t)chain, L);
-    cpx<T> nC[JPL], nS[JPL];
+    cpx<T> nT[JPL];
+    const T nRowRe = rowLogC[dn.site].re;
 #pragma unroll
     for (int q = 0; q < JPL; ++q) {
       const int j = lane + 32 * q;
-      nC[q] = j < M ? tC[(size_t)dn.site * M + j] : mk(T(1), T(0));
-      nS[q] = j < M ? tS[(size_t)dn.site * M + j] : mk(T(0), T(0));
+      nT[q] = j < M ? tT[(size_t)dn.site * M + j] : mk(T(0), T(0));
     }
     const T sg = cfg[i] ? T(1) : T(-1);
-    // |ratio|^2 over this lane's hidden units, as mantissa * 2^ex
+    // |ratio / prod_j cosh 2W_ij|^2 over this lane's hidden units, as mantissa * 2^ex
     T prod = T(1);
     int ex = 0;
 #pragma unroll
     for (int q = 0; q < JPL; ++q) {
       const int j = lane + 32 * q;
       if (j < M) {
-        cpx<T> f = fC[q] - sg * (tn[q] * fS[q]);
-        prod *= abs2(f);
+        const cpx<T> g = tn[q] * fT[q];
+        prod *= abs2(mk(T(1) - sg * g.re, -sg * g.im));
         if ((q & 3) == 3) {
           int e = exponent_of(prod);
           if (prod != T(0) && isfinite(prod)) {
@@ -758,12 +763,13 @@ __global__ void __launch_bounds__(256) rbm_metropolis_kernel(
     ex = __shfl_sync(0xffffffffu, ex, 0);
     bool acc;
     if (sizeof(T) == sizeof(double)) {
-      // P = |ratio|^mu = (prod * 2^ex)^(mu/2); accept iff u < P (bernoulli, sampler.py:339-340)
-      const double logr2 = log((double)prod) + (double)ex * 0.69314718055994530942;
+      // P = |ratio|^mu = (prod * 2^ex * exp(2 Re rowLogC))^(mu/2); accept iff
+      // u < P (bernoulli, sampler.py:339-340)
+      const double logr2 = log((double)prod) + (double)ex * 0.69314718055994530942 + 2.0 * (double)rowRe;
       const double P = exp((double)halfMu * logr2);
       acc = d.u64() < P;
     } else {
-      const float lg2 = log2f((float)prod) + (float)ex;
+      const float lg2 = log2f((float)prod) + (float)ex + 2.8853900817779268f * (float)rowRe;
       const float P = exp2f((float)halfMu * lg2);
       acc = d.u32() < P;
     }
@@ -783,10 +789,8 @@ __global__ void __launch_bounds__(256) rbm_metropolis_kernel(
       ++accepted;
     }
 #pragma unroll
-    for (int q = 0; q < JPL; ++q) {
-      fC[q] = nC[q];
-      fS[q] = nS[q];
-    }
+    for (int q = 0; q < JPL; ++q) fT[q] = nT[q];
+    rowRe = nRowRe;
     d = dn;
     if (step >= thermSteps && ((step - thermSteps + 1) % sweepSteps) == 0) {
       const int64_t s = (step - thermSteps + 1) / sweepSteps - 1;
