@@ -26,7 +26,8 @@ def _split_product(ah, al, bh, bl, k):
     return a_h @ b_h.T + a_h @ b_l.T + a_l @ b_h.T
 
 
-@pytest.mark.parametrize("rows,k", [(200, 300), (600, 1000), (128, 64), (1000, 2048)])
+# (2600, 256): 11 column tiles = a full and a ragged group of the tile order
+@pytest.mark.parametrize("rows,k", [(200, 300), (600, 1000), (128, 64), (1000, 2048), (2600, 256)])
 def test_gram_bf16x3(cuda, rows, k):
     import vmc_jax_gb300._lib as L
     torch.manual_seed(rows + k)
@@ -50,7 +51,7 @@ def test_gram_bf16x3(cuda, rows, k):
     assert (got - full).abs().max() / full.abs().max() < 1e-4
 
 
-@pytest.mark.parametrize("m,n,k", [(300, 520, 200), (1024, 256, 512), (77, 1000, 130)])
+@pytest.mark.parametrize("m,n,k", [(300, 520, 200), (1024, 256, 512), (77, 1000, 130), (700, 2600, 192)])
 def test_gemm_bf16x3_colsq(cuda, m, n, k):
     import vmc_jax_gb300._lib as L
     torch.manual_seed(m * n + k)

@@ -11,14 +11,17 @@
 //            representation of the eigenvectors; D is never stored.
 //
 // Every operand x is given as two BF16 planes x ~ hi + lo and the product is
-// formed as hi.hi + hi.lo + lo.hi (three passes over K accumulating into the
-// same FP32 TMEM tile): about 16 significant bits per operand instead of 8.
+// formed as hi.hi + hi.lo + lo.hi accumulating into the same FP32 TMEM tile:
+// about 16 significant bits per operand instead of 8.
 //
-// Tile: 128 x 256 x 64 (one tcgen05.mma M=128 N=256 per 16-wide K slice),
-// 4-stage TMA -> shared memory ring (128-byte swizzle, K-major).  Warp 0:
-// TMA producer; warp 1: TMEM owner and MMA issuer; warps 2-5: epilogue
-// (tcgen05.ld of the 128 x 256 FP32 accumulator).  All mbarrier waits are
-// bounded; a timeout sets vmc_tc_error and the CTA unwinds.
+// Tile: 128 x 256 x 64 (one tcgen05.mma M=128 N=256 per 16-wide K slice).
+// A pipeline stage holds all four operand tiles of one 64-wide K block
+// (A hi, A lo, B hi, B lo: 96 KB), so each plane is read from L2 once per K
+// block and the stage feeds 12 MMAs (3 products x 4 slices); 2-stage TMA ->
+// shared memory ring (128-byte swizzle, K-major).  Warp 0: TMA producer;
+// warp 1: TMEM owner and MMA issuer; warps 2-5: epilogue (tcgen05.ld of the
+// 128 x 256 FP32 accumulator).  All mbarrier waits are bounded; a timeout
+// sets vmc_tc_error and the CTA unwinds.
 #include <cuda.h>
 #include <cuda_bf16.h>
 
@@ -28,10 +31,10 @@
 
 namespace vmc {
 
-constexpr int TC_BM = 128, TC_BN = 256, TC_BK = 64, TC_STAGES = 4;
-constexpr int TC_A_BYTES = TC_BM * TC_BK * 2;          // 16 KB
-constexpr int TC_B_BYTES = TC_BN * TC_BK * 2;          // 32 KB
-constexpr int TC_STAGE_BYTES = TC_A_BYTES + TC_B_BYTES;  // 48 KB
+constexpr int TC_BM = 128, TC_BN = 256, TC_BK = 64, TC_STAGES = 2;
+constexpr int TC_A_BYTES = TC_BM * TC_BK * 2;                 // 16 KB per plane
+constexpr int TC_B_BYTES = TC_BN * TC_BK * 2;                 // 32 KB per plane
+constexpr int TC_STAGE_BYTES = 2 * TC_A_BYTES + 2 * TC_B_BYTES;  // 96 KB: A hi, A lo, B hi, B lo
 constexpr int TC_SMEM = TC_STAGES * TC_STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
 constexpr int TC_THREADS = 192;
 constexpr uint32_t TC_TMEM_COLS = 256;
@@ -139,24 +142,71 @@ struct tc_args {
   int64_t ldOut;
 };
 
-// Upper-triangle tile enumeration for the symmetric product: column tile tn
-// holds the row tiles tm with tm * BM <= tn * BN + BN - 1, i.e. tm < 2 tn + 2
-// (BN = 2 BM), capped at tilesM.
-__device__ __forceinline__ void sym_tile(int b, int tilesM, int& tm, int& tn) {
-  // columns with a full triangle prefix: count(tn) = tn (tn + 1) while 2 tn + 2 <= tilesM
-  const int T0 = tilesM / 2;  // columns 0..T0-1 have 2tn+2 <= tilesM tiles
-  const int prefix = T0 * (T0 + 1);
-  if (b < prefix) {
-    int t = (int)((sqrtf(4.0f * (float)b + 1.0f) - 1.0f) * 0.5f);
-    while (t * (t + 1) > b) --t;
-    while ((t + 1) * (t + 2) <= b) ++t;
-    tn = t;
-    tm = b - t * (t + 1);
-  } else {
-    const int r = b - prefix;
-    tn = T0 + r / tilesM;
-    tm = r - (r / tilesM) * tilesM;
+// Tile order.  Column tiles are taken in groups of TC_GROUP; inside a group
+// the tiles run row by row (tm outer, tn inner), so the CTAs resident at one
+// time cover about 19 row tiles x 8 column tiles and share their operand
+// panels through L2 (a column-at-a-time order streams ~150 distinct A panels
+// per wave from DRAM).
+//
+// Symmetric product (mode 0): only tiles touching the upper triangle,
+// column tile tn holds the row tiles tm < 2 tn + 2 (BN = 2 BM), capped at
+// tilesM; equivalently row tm meets the column tiles tn >= tm / 2.  A group
+// [c0, c1) has full rows tm < min(R, 2 c0) (all w = c1 - c0 tiles) and at
+// most 2 w ragged rows after them, R = min(tilesM, 2 c1).
+constexpr int TC_GROUP = 8;
+
+__host__ __device__ inline int sym_group_size(int c0, int c1, int tilesM, int& full) {
+  const int R = tilesM < 2 * c1 ? tilesM : 2 * c1;
+  full = R < 2 * c0 ? R : 2 * c0;
+  int n = (c1 - c0) * full;
+  for (int tm = full; tm < R; ++tm) n += c1 - tm / 2;
+  return n;
+}
+
+__host__ __device__ inline void tile_of(int b, int mode, int tilesM, int tilesN, int& tm, int& tn) {
+  if (mode != 0) {
+    const int per = TC_GROUP * tilesM;
+    const int g = b / per, o = b - g * per;
+    const int c0 = g * TC_GROUP;
+    const int w = tilesN - c0 < TC_GROUP ? tilesN - c0 : TC_GROUP;
+    tm = o / w;
+    tn = c0 + (o - tm * w);
+    return;
   }
+  int o = b;
+  for (int c0 = 0; c0 < tilesN; c0 += TC_GROUP) {
+    const int c1 = c0 + TC_GROUP < tilesN ? c0 + TC_GROUP : tilesN;
+    int full;
+    const int n = sym_group_size(c0, c1, tilesM, full);
+    if (o >= n) {
+      o -= n;
+      continue;
+    }
+    const int w = c1 - c0;
+    if (o < w * full) {
+      tm = o / w;
+      tn = c0 + (o - tm * w);
+      return;
+    }
+    o -= w * full;
+    for (int r = full;; ++r) {
+      const int cnt = c1 - r / 2;
+      if (o < cnt) {
+        tm = r;
+        tn = r / 2 + o;
+        return;
+      }
+      o -= cnt;
+    }
+  }
+  tm = tn = 0;  // not reached for b < number of tiles
+}
+
+__host__ inline int64_t tile_count(int mode, int tilesM, int tilesN) {
+  if (mode != 0) return (int64_t)tilesM * tilesN;
+  int64_t n = 0;
+  for (int tn = 0; tn < tilesN; ++tn) n += tilesM < 2 * tn + 2 ? tilesM : 2 * tn + 2;
+  return n;
 }
 
 __global__ void __launch_bounds__(TC_THREADS, 1)
@@ -172,12 +222,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
   int tm, tn;
-  if (a.mode == 0) {
-    sym_tile(blockIdx.x, a.tilesM, tm, tn);
-  } else {
-    tm = blockIdx.x % a.tilesM;
-    tn = blockIdx.x / a.tilesM;
-  }
+  tile_of(blockIdx.x, a.mode, a.tilesM, a.tilesN, tm, tn);
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < TC_STAGES; ++s) {
@@ -200,7 +245,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   const uint32_t tmem = *tmemSlot;
 
   const int nkb = (a.K + TC_BK - 1) / TC_BK;
-  const int iters = 3 * nkb;  // passes: hi.hi, hi.lo, lo.hi
+  const int iters = nkb;  // one stage per K block, all three products
   bool ok = true;
 
   if (warp == 0) {
@@ -213,12 +258,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         if (!ok) break;
         const uint32_t full = smem_u32(&bars[s]);
         mbar_expect_tx(full, TC_STAGE_BYTES);
-        const int pass = it / nkb, kb = it - pass * nkb;
-        const CUtensorMap* mA = pass == 2 ? &mapAlo : &mapAhi;
-        const CUtensorMap* mB = pass == 1 ? &mapBlo : &mapBhi;
+        const int kb = it;
         unsigned char* st = smem + s * TC_STAGE_BYTES;
-        tma_load_2d(smem_u32(st), mA, kb * TC_BK, tm * TC_BM, full);
-        tma_load_2d(smem_u32(st + TC_A_BYTES), mB, kb * TC_BK, tn * TC_BN, full);
+        tma_load_2d(smem_u32(st), &mapAhi, kb * TC_BK, tm * TC_BM, full);
+        tma_load_2d(smem_u32(st + TC_A_BYTES), &mapAlo, kb * TC_BK, tm * TC_BM, full);
+        tma_load_2d(smem_u32(st + 2 * TC_A_BYTES), &mapBhi, kb * TC_BK, tn * TC_BN, full);
+        tma_load_2d(smem_u32(st + 2 * TC_A_BYTES + TC_B_BYTES), &mapBlo, kb * TC_BK, tn * TC_BN, full);
         ++issued;
       }
       if (!ok) {
@@ -237,12 +282,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         if (!ok) break;
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         unsigned char* st = smem + s * TC_STAGE_BYTES;
-        const uint64_t da = smem_desc_sw128(smem_u32(st));
-        const uint64_t db = smem_desc_sw128(smem_u32(st + TC_A_BYTES));
+        const uint64_t dah = smem_desc_sw128(smem_u32(st));
+        const uint64_t dal = smem_desc_sw128(smem_u32(st + TC_A_BYTES));
+        const uint64_t dbh = smem_desc_sw128(smem_u32(st + 2 * TC_A_BYTES));
+        const uint64_t dbl = smem_desc_sw128(smem_u32(st + 2 * TC_A_BYTES + TC_B_BYTES));
 #pragma unroll
         for (int k = 0; k < TC_BK / 16; ++k) {
           // advance the start address by k * 16 bf16 = 32 bytes inside the swizzle atom
-          mma_bf16(tmem, da + (uint64_t)(2 * k), db + (uint64_t)(2 * k), idesc, (it > 0 || k > 0) ? 1u : 0u);
+          const uint64_t o = (uint64_t)(2 * k);
+          mma_bf16(tmem, dah + o, dbh + o, idesc, (it > 0 || k > 0) ? 1u : 0u);
+          mma_bf16(tmem, dah + o, dbl + o, idesc, 1u);
+          mma_bf16(tmem, dal + o, dbh + o, idesc, 1u);
         }
         mma_commit(smem_u32(&bars[TC_STAGES + s]));
       }
@@ -369,10 +419,7 @@ extern "C" int vmc_gram_bf16x3(const void* hi, const void* lo, int32_t rows, int
   a.tilesN = (rows + TC_BN - 1) / TC_BN;
   a.out = gram;
   a.ldOut = ld_gram;
-  // tiles with tm < 2 tn + 2, capped at tilesM
-  int64_t grid = 0;
-  for (int tn = 0; tn < a.tilesN; ++tn) grid += std::min(a.tilesM, 2 * tn + 2);
-  return launch_tc(mh, ml, nh, nl, a, (int)grid, as_stream(stream));
+  return launch_tc(mh, ml, nh, nl, a, (int)tile_count(0, a.tilesM, a.tilesN), as_stream(stream));
 }
 
 namespace vmc {
@@ -412,7 +459,7 @@ extern "C" int vmc_gemm_bf16x3_colsq(const void* a_hi, const void* a_lo, int32_t
   a.tilesN = (n + TC_BN - 1) / TC_BN;
   a.out = reinterpret_cast<float*>(workspace);
   a.ldOut = 0;
-  int rc2 = launch_tc(ah, al, bh, bl, a, a.tilesM * a.tilesN, as_stream(stream));
+  int rc2 = launch_tc(ah, al, bh, bl, a, (int)tile_count(1, a.tilesM, a.tilesN), as_stream(stream));
   if (rc2) return rc2;
   colsq_reduce_kernel<<<(n + 255) / 256, 256, 0, as_stream(stream)>>>(reinterpret_cast<const float*>(workspace),
                                                                        a.tilesM * 4, n, colsq);
