@@ -721,13 +721,13 @@ def main():
         peak = peaks.get("bf16_tflops_sustained", 1700.0)
         ach = flops / t / 1e12
         # DRAM traffic of one launch, scaled from the ncu capture of the same
-        # kernel at rows 8192, K 16384 (profiles/tc_gemm_gram_rows8192_k16384.md:
-        # 4.689 GB read + 0.123 GB written over 1056 tiles of 128 x 256): per
-        # tile the operand panels grow with K, the FP32 tile write does not
+        # kernel at rows 8192, K 16384 (2.065 GB read + 0.123 GB written over
+        # 1056 tiles of 128 x 256, grouped tile order): per tile the operand
+        # panels grow with K, the FP32 tile write does not
         R = 2 * P
         tilesM, tilesN = (R + 127) // 128, (R + 255) // 256
         tiles = sum(min(tilesM, 2 * tn + 2) for tn in range(tilesN))
-        traffic = tiles * (4.688826e9 / 1056 * (Ns / 16384.0) + 0.122841e9 / 1056)
+        traffic = tiles * (2.065120e9 / 1056 * (Ns / 16384.0) + 0.122942e9 / 1056)
         roofline = {"kernel": "tc_gemm_kernel (S build, BF16x3 split, tcgen05)", "bound": "tensor",
                     "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
                     "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained (of measured)",
