@@ -380,7 +380,10 @@ def kernel_bench(args):
     gram  tcgen05 BF16x3 Gram, rows 8192 x K 16384 (planes 537 MB > L2)
     snr   tcgen05 BF16x3 colsq GEMM, 16384 x 8192 x 8192
     eloc  fused E_loc of the L=64, M=256 Ising workload, 16384 samples
-    metropolis  RBM Metropolis, 1024 chains, L=64, M=256, 64 sweeps"""
+    metropolis  RBM Metropolis, 1024 chains, L=64, M=256, 64 sweeps
+    data  centred O_k as transposed BF16 hi/lo planes, N=16384, L=64, M=256
+    hermitian, gemv, stats  the TDVP solve's FP32 -> Hermitian fill, U^H x / U x,
+          and the FP64 O_k statistics"""
     import torch
     import vmc_jax_gb300 as V
     L_ = V._lib
@@ -419,8 +422,9 @@ def kernel_bench(args):
         unit, bound = "GB/s", "hbm"
         alg = hw = None
         if args.kernel == "data":
-            # centred O_k -> transposed BF16 hi/lo planes: N=16384, L=64, M=64 (P=4160)
-            N, L, M = 16384, 64, 64
+            # centred O_k -> transposed BF16 hi/lo planes of the 64-site step:
+            # N=16384, L=64, M=256 (P=16640; planes 2.18 GB)
+            N, L, M = 16384, 64, 256
             P = L * M + M
             cfg_ = torch.randint(0, 2, (N, L), dtype=torch.int32, device=dev, generator=g)
             W = (0.05 * torch.randn(L, M, dtype=torch.complex64, device=dev, generator=g)).contiguous()

@@ -18,34 +18,53 @@
 namespace vmc {
 
 
-// tanh(theta) of kTileN samples into shared memory (as T), one warp per sample.
-template <typename T>
+// tanh(theta) of the tile's kTileN (<= 32) samples into shared memory (as T).
+// Thread -> hidden unit j; every W_ij is loaded once per pass of S samples
+// and applied to S accumulators in registers, the signs taken from a per-site
+// bit mask of the tile's configurations (bit r = s_i of sample r).  Each
+// theta is summed in the order b_j, then i = 0 .. L-1, as in rbm_logpsi.
+template <typename T, int S>
 __device__ void tile_tanh(const int32_t* __restrict__ configs, int64_t n0, int64_t N, int L, int M,
                           const cpx<T>* __restrict__ W, const cpx<T>* __restrict__ b, cpx<T>* tt, int8_t* sg,
-                          int kTileN) {
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
-  for (int r = warp; r < kTileN; r += nwarps) {
+                          uint32_t* sbits, int kTileN) {
+  const int tid = threadIdx.x;
+  for (int idx = tid; idx < kTileN * L; idx += blockDim.x) {
+    const int r = idx / L, i = idx - r * L;
     const int64_t n = n0 + r;
-    int8_t* cfg = sg + r * (L + 1);
-    if (n < N) {
-      for (int i = lane; i < L; i += 32) cfg[i] = (int8_t)configs[n * L + i];
-    } else {
-      for (int i = lane; i < L; i += 32) cfg[i] = 0;
-    }
-    __syncwarp();
-    for (int j = lane; j < M; j += 32) {
-      cpx<T> th = b ? b[j] : mk(T(0), T(0));
+    sg[r * (L + 1) + i] = n < N ? (int8_t)(configs[n * L + i] != 0) : (int8_t)0;
+  }
+  __syncthreads();
+  for (int i = tid; i < L; i += blockDim.x) {
+    uint32_t m = 0;
+    for (int r = 0; r < kTileN; ++r) m |= (uint32_t)sg[r * (L + 1) + i] << r;
+    sbits[i] = m;
+  }
+  __syncthreads();
+  for (int s0 = 0; s0 < kTileN; s0 += S) {
+    for (int j = tid; j < M; j += blockDim.x) {
+      const cpx<T> bj = b ? b[j] : mk(T(0), T(0));
+      T ar[S], ai[S];
+#pragma unroll
+      for (int s = 0; s < S; ++s) {
+        ar[s] = bj.re;
+        ai[s] = bj.im;
+      }
+#pragma unroll 4
       for (int i = 0; i < L; ++i) {
-        cpx<T> x = W[(size_t)i * M + j];
-        if (cfg[i]) {
-          th.re += x.re;
-          th.im += x.im;
-        } else {
-          th.re -= x.re;
-          th.im -= x.im;
+        const cpx<T> x = W[(size_t)i * M + j];
+        const uint32_t m = sbits[i] >> s0;
+#pragma unroll
+        for (int s = 0; s < S; ++s) {
+          const bool up = (m >> s) & 1u;
+          ar[s] += up ? x.re : -x.re;
+          ai[s] += up ? x.im : -x.im;
         }
       }
-      tt[(size_t)r * (M + 1) + j] = n < N ? ctanh_(th) : mk(T(0), T(0));
+#pragma unroll
+      for (int s = 0; s < S; ++s) {
+        const int r = s0 + s;
+        if (r < kTileN) tt[(size_t)r * (M + 1) + j] = n0 + r < N ? ctanh_(mk(ar[s], ai[s])) : mk(T(0), T(0));
+      }
     }
   }
   __syncthreads();
@@ -154,6 +173,7 @@ __global__ void __launch_bounds__(256) rbm_data_kernel(const int32_t* __restrict
   float2* cforce = cmean + a.colChunk;
   float2* sxde = cforce + a.colChunk;
   float* ssw = reinterpret_cast<float*>(sxde + kTileN);
+  uint32_t* sbits = reinterpret_cast<uint32_t*>(ssw + kTileN);
   const int64_t n0 = (int64_t)blockIdx.x * kTileN;
   const int P = a.M * a.L + (a.hasBias ? a.M : 0);
   const int k0 = blockIdx.y * a.colChunk, k1 = min(P, k0 + a.colChunk);
@@ -178,7 +198,8 @@ __global__ void __launch_bounds__(256) rbm_data_kernel(const int32_t* __restrict
       }
     }
   }
-  tile_tanh<T>(configs, n0, a.N, a.L, a.M, W, b, tt, sg, kTileN);  // ends with __syncthreads
+  // ends with __syncthreads; S accumulators per pass: 16 FP32 or 8 FP64 complex
+  tile_tanh<T, sizeof(T) == 4 ? 16 : 8>(configs, n0, a.N, a.L, a.M, W, b, tt, sg, sbits, kTileN);
   const float2 zero2 = make_float2(0.f, 0.f);
   if (a.format == VMC_DATA_BF16X2 && a.eloc == nullptr) {
     // transposed planes (2P, N): thread -> (sample lane r, column group)
@@ -249,12 +270,14 @@ static int launch_data(int32_t precision, const int32_t* configs, const void* ke
                 (long long)need);
   }
   const size_t el = precision == VMC_F64 ? 16 : 8;
-  int kTileN = 64;
-  while (kTileN > 8 && (size_t)kTileN * ((a.M + 1) * el + a.L + 1) > 180 * 1024) kTileN /= 2;
+  // at most 32 samples per tile (one bit each in the per-site sign masks);
+  // fewer when the tile's tanh values would not leave room for two blocks
+  int kTileN = 32;
+  while (kTileN > 8 && (size_t)kTileN * ((a.M + 1) * el + a.L + 1) > 96 * 1024) kTileN /= 2;
   a.tileN = kTileN;
   a.colChunk = 2048;
   const size_t tileBytes = ((size_t)kTileN * (a.M + 1) * el + (size_t)kTileN * (a.L + 1) + 15) & ~(size_t)15;
-  const size_t smem = tileBytes + (size_t)a.colChunk * 16 + (size_t)kTileN * 12;
+  const size_t smem = tileBytes + (size_t)a.colChunk * 16 + (size_t)kTileN * 12 + (size_t)a.L * 4;
   VMC_REQUIRE(smem <= 227 * 1024, VMC_ERR_UNSUPPORTED, "%s: M=%d, L=%d too large for one tile", fn, a.M, a.L);
   // columns split over grid y so that enough blocks are resident; each block
   // recomputes tanh(theta) of its samples (L M per sample, small next to the
