@@ -159,6 +159,15 @@ __device__ __forceinline__ void store_split(__nv_bfloat16* hi, __nv_bfloat16* lo
   lo[idx] = __float2bfloat16_rn(v - __bfloat162float(h));
 }
 
+// two adjacent elements (idx even) with one 4-byte store per plane; the same
+// values as two store_split calls
+__device__ __forceinline__ void store_split2(__nv_bfloat16* hi, __nv_bfloat16* lo, size_t idx, float v0, float v1) {
+  const __nv_bfloat162 h = __floats2bfloat162_rn(v0, v1);
+  const float2 hf = __bfloat1622float2(h);
+  *reinterpret_cast<__nv_bfloat162*>(hi + idx) = h;
+  *reinterpret_cast<__nv_bfloat162*>(lo + idx) = __floats2bfloat162_rn(v0 - hf.x, v1 - hf.y);
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) rbm_data_kernel(const int32_t* __restrict__ configs, const cpx<T>* __restrict__ W,
                                                        const cpx<T>* __restrict__ b, data_args a) {
@@ -201,10 +210,42 @@ __global__ void __launch_bounds__(256) rbm_data_kernel(const int32_t* __restrict
   // ends with __syncthreads; S accumulators per pass: 16 FP32 or 8 FP64 complex
   tile_tanh<T, sizeof(T) == 4 ? 16 : 8>(configs, n0, a.N, a.L, a.M, W, b, tt, sg, sbits, kTileN);
   const float2 zero2 = make_float2(0.f, 0.f);
+  // BF16 planes whose leading dimension and bases allow 4-byte stores of
+  // element pairs
+  const bool pairs = a.format == VMC_DATA_BF16X2 && (a.ld & 1) == 0 &&
+                     ((reinterpret_cast<uintptr_t>(a.out) | reinterpret_cast<uintptr_t>(a.out2)) & 3) == 0;
   if (a.format == VMC_DATA_BF16X2 && a.eloc == nullptr) {
-    // transposed planes (2P, N): thread -> (sample lane r, column group)
+    // transposed planes (2P, N)
     __nv_bfloat16* hi = reinterpret_cast<__nv_bfloat16*>(a.out);
     __nv_bfloat16* lo = reinterpret_cast<__nv_bfloat16*>(a.out2);
+    if (pairs) {
+      // thread -> (sample pair r, r + 1; column group): samples are adjacent
+      // in a plane row, so one store carries both
+      const int half = kTileN / 2;
+      const int r = 2 * (tid % half);
+      const int cg = tid / half, ncg = blockDim.x / half;
+      const int64_t n = n0 + r;
+      if (n < a.N) {
+        const bool two = n + 1 < a.N;
+        const float sw0 = ssw[r], sw1 = ssw[r + 1];
+        col_pos c;
+        c.set(k0 + cg, a.M, a.hasBias);
+        for (int k = k0 + cg; k < k1; k += ncg, c.advance(ncg, a.M)) {
+          const float2 mu = cmean[k - k0];
+          const cpx<float> v0 = data_value_f<T>(a, tt, sg, r, c, mu, zero2, sw0, zero2);
+          if (two) {
+            const cpx<float> v1 = data_value_f<T>(a, tt, sg, r + 1, c, mu, zero2, sw1, zero2);
+            store_split2(hi, lo, (size_t)k * a.ld + n, v0.re, v1.re);
+            store_split2(hi, lo, (size_t)(P + k) * a.ld + n, v0.im, v1.im);
+          } else {
+            store_split(hi, lo, (size_t)k * a.ld + n, v0.re);
+            store_split(hi, lo, (size_t)(P + k) * a.ld + n, v0.im);
+          }
+        }
+      }
+      return;
+    }
+    // thread -> (sample lane r, column group)
     const int r = tid % kTileN;
     const int cg = tid / kTileN, ncg = blockDim.x / kTileN;
     const int64_t n = n0 + r;
@@ -236,6 +277,29 @@ __global__ void __launch_bounds__(256) rbm_data_kernel(const int32_t* __restrict
     }
     const float sw = ssw[r];
     const float2 xde = a.eloc ? sxde[r] : zero2;
+    if (pairs && (P & 1) == 0) {
+      // BF16X2 row-major (N, 2P): thread -> column pair k, k + 1 (k0 and P
+      // even, so both halves of the row start on an even element)
+      __nv_bfloat16* hi = reinterpret_cast<__nv_bfloat16*>(a.out);
+      __nv_bfloat16* lo = reinterpret_cast<__nv_bfloat16*>(a.out2);
+      c.set(k0 + 2 * tid, a.M, a.hasBias);
+      for (int k = k0 + 2 * tid; k < k1; k += 2 * blockDim.x, c.advance(2 * blockDim.x, a.M)) {
+        const cpx<float> v0 =
+            data_value_f<T>(a, tt, sg, r, c, cmean[k - k0], a.eloc ? cforce[k - k0] : zero2, sw, xde);
+        if (k + 1 < k1) {
+          col_pos c1 = c;
+          c1.advance(1, a.M);
+          const cpx<float> v1 = data_value_f<T>(a, tt, sg, r, c1, cmean[k + 1 - k0],
+                                                a.eloc ? cforce[k + 1 - k0] : zero2, sw, xde);
+          store_split2(hi, lo, n * a.ld + k, v0.re, v1.re);
+          store_split2(hi, lo, n * a.ld + P + k, v0.im, v1.im);
+        } else {
+          store_split(hi, lo, n * a.ld + k, v0.re);
+          store_split(hi, lo, n * a.ld + P + k, v0.im);
+        }
+      }
+      continue;
+    }
     for (int k = k0 + tid; k < k1; k += blockDim.x, c.advance(blockDim.x, a.M)) {
       const cpx<float> v =
           data_value_f<T>(a, tt, sg, r, c, cmean[k - k0], a.eloc ? cforce[k - k0] : zero2, sw, xde);
