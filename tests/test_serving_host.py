@@ -1,0 +1,144 @@
+"""Host logic of the serving loop (vmc_jax_gb300.serving.Server) on the CPU:
+admission against the slot count and the HBM budget, per-job failure,
+cancellation and the report, with the device side (slot buffers, the shared
+sampling graph, the FP64 solve) replaced by a stand-in that sleeps.  The
+GPU path itself is covered by tests/test_gpu_serving.py."""
+
+import threading
+import time
+
+import pytest
+import torch
+
+from vmc_jax_gb300 import serving
+
+
+class FakeSlot:
+    """A job's step: sleeps, records an energy, calls on_step; a job whose
+    seed is 13 raises in its second step."""
+
+    def __init__(self, job_id, spec, arrival_wall):
+        self.id = job_id
+        self.spec = spec
+        self.arrival_wall = arrival_wall
+        self.steps_done = 0
+        self.step_latencies = []
+        self.energies = []
+        self.theta = torch.zeros(4, dtype=torch.float64)
+
+    def solve(self, ready_event, t_launch):
+        time.sleep(0.002)
+        if self.spec.seed == 13 and self.steps_done == 1:
+            raise RuntimeError("planted failure")
+        self.energies.append(torch.tensor(-float(self.steps_done)))
+        self.theta = self.theta + 1.0
+        self.steps_done += 1
+        self.step_latencies.append(time.perf_counter() - t_launch)
+        if self.spec.on_step is not None:
+            self.spec.on_step(self.id, self.steps_done, float(self.energies[-1]))
+
+    @property
+    def finished(self):
+        return self.steps_done >= self.spec.steps
+
+
+class HostServer(serving.Server):
+    def __init__(self, **kw):
+        self.launched = []
+        self.resident_seen = []
+        super().__init__(**kw)
+
+    def _open_device(self):
+        return None
+
+    def _new_slot(self, job_id, spec, arrival_wall):
+        return FakeSlot(job_id, spec, arrival_wall)
+
+    def _launch(self, ids):
+        self.launched.append(tuple(ids))
+        self.resident_seen.append(len(self.active))
+        return None, time.perf_counter()
+
+
+def _spec(steps=3, **kw):
+    return serving.JobSpec(L=8, h=1.0, M=8, num_samples=256, steps=steps, **kw)
+
+
+def _run(server, timeout=60.0):
+    out = {}
+    th = threading.Thread(target=lambda: out.setdefault("report", server.run()), daemon=True)
+    th.start()
+    th.join(timeout)
+    assert not th.is_alive(), "serving loop did not finish"
+    return out["report"]
+
+
+def test_all_jobs_complete_in_order():
+    srv = HostServer(hbm_budget=1 << 40, max_slots=4, batch_window=0.0)
+    seen = {}
+    cb = lambda jid, step, e: seen.setdefault(jid, []).append(step)
+    ids = [srv.submit(_spec(steps=3 + i % 2, arrival=0.001 * i, on_step=cb)) for i in range(6)]
+    rep = _run(srv)
+    assert rep["jobs"] == 6 and rep["not_completed"] == {}
+    assert rep["steps"] == sum(3 + i % 2 for i in range(6))
+    assert all(srv.status(i) == "done" for i in ids)
+    for i in ids:
+        assert seen[i] == list(range(1, srv.done[i].spec.steps + 1))
+        theta, energies = srv.result(i)
+        assert energies.shape[0] == srv.done[i].spec.steps
+    assert max(srv.resident_seen) <= 4 and rep["max_resident_jobs"] <= 4
+    assert rep["graph_launches"] == len(srv.launched)
+
+
+def test_budget_rejects_and_defers():
+    one = serving.footprint_bytes(_spec())
+    srv = HostServer(hbm_budget=2 * one + 1, max_slots=8, batch_window=0.0)
+    big = serving.JobSpec(L=64, h=1.0, M=256, num_samples=16384, steps=1)
+    assert serving.footprint_bytes(big) > srv.hbm_budget
+    jb = srv.submit(big)
+    small = [srv.submit(_spec()) for _ in range(5)]
+    rep = _run(srv)
+    assert srv.status(jb) == "rejected" and "HBM budget" in srv.errors[jb]
+    assert all(srv.status(i) == "done" for i in small)
+    assert rep["max_resident_jobs"] == 2  # two footprints fit the budget at a time
+    assert rep["not_completed"] == {jb: "rejected"}
+    with pytest.raises(KeyError, match="rejected"):
+        srv.result(jb)
+
+
+def test_failure_stays_with_its_job():
+    srv = HostServer(hbm_budget=1 << 40, max_slots=4, batch_window=0.0)
+    bad = srv.submit(_spec(steps=4, seed=13))
+    good = [srv.submit(_spec(steps=4, seed=s)) for s in range(3)]
+    rep = _run(srv)
+    assert srv.status(bad) == "failed" and "planted failure" in srv.errors[bad]
+    assert all(srv.status(i) == "done" for i in good)
+    assert rep["jobs"] == 3 and rep["steps"] == 12
+
+
+def test_cancel_queued_and_active():
+    srv = HostServer(hbm_budget=1 << 40, max_slots=2, batch_window=0.0)
+
+    def stop_after_two(jid, step, e):
+        if step == 2:
+            srv.cancel(jid)
+
+    active = srv.submit(_spec(steps=10, on_step=stop_after_two))
+    late = srv.submit(_spec(steps=2, arrival=30.0))  # not yet arrived: still queued
+    other = srv.submit(_spec(steps=3))
+    srv.cancel(late)
+    assert srv.status(late) == "cancelled"
+    rep = _run(srv)
+    assert srv.status(active) == "cancelled"
+    assert srv.status(other) == "done"
+    assert rep["not_completed"] == {active: "cancelled", late: "cancelled"}
+
+
+def test_invalid_specs_are_refused_at_submit():
+    srv = HostServer(hbm_budget=1 << 30)
+    for bad in (serving.JobSpec(L=1, h=1.0, M=4, num_samples=64),
+                serving.JobSpec(L=8, h=1.0, M=4, num_samples=64, kind="annealing"),
+                serving.JobSpec(L=8, h=1.0, M=4, num_samples=64, precision="fp16")):
+        with pytest.raises(ValueError):
+            srv.submit(bad)
+    assert srv.states == {}

@@ -204,7 +204,7 @@ class Server:
     ``batch_window``: seconds a tick waits for more jobs to become ready."""
 
     def __init__(self, hbm_budget=None, max_slots=8, batch_window=0.002):
-        _lib.require_cuda()
+        self.sample_stream = self._open_device()
         if hbm_budget is None:
             free, _ = torch.cuda.mem_get_info()
             hbm_budget = int(0.8 * free)
@@ -219,7 +219,6 @@ class Server:
         self.ready = set()
         self.next_id = 0
         self.t0 = None
-        self.sample_stream = torch.cuda.Stream()
         self.max_resident = 0
         self.graph_launches = 0
         self.states = {}        # job id -> queued / active / done / failed / rejected / cancelled
@@ -252,6 +251,27 @@ class Server:
     def status(self, job_id):
         return self.states.get(job_id)
 
+    # ---- the device side of the loop (the scheduling above and below is
+    # host logic only)
+    def _open_device(self):
+        """Check for the CUDA library and return the stream the shared graphs run on."""
+        _lib.require_cuda()
+        return torch.cuda.Stream()
+
+    def _new_slot(self, job_id, spec, arrival_wall):
+        return _Slot(job_id, spec, arrival_wall)
+
+    def _launch(self, ids):
+        """Replay the sampling + E_loc graph of the ready jobs ``ids``; returns
+        the event the jobs' solves wait on and the launch time."""
+        g = self._graph_for(ids)
+        t_launch = time.perf_counter()
+        with torch.cuda.stream(self.sample_stream):
+            g.replay()
+            ev = torch.cuda.Event()
+            ev.record(self.sample_stream)
+        return ev, t_launch
+
     def _used(self):
         return sum(footprint_bytes(s.spec) for s in self.active.values())
 
@@ -273,7 +293,7 @@ class Server:
                 continue
             self.queue.remove(item)
             try:
-                slot = _Slot(jid, spec, self.t0 + spec.arrival)
+                slot = self._new_slot(jid, spec, self.t0 + spec.arrival)
             except Exception as e:  # e.g. device memory exhausted while allocating the slot
                 self.states[jid] = "failed"
                 self.errors[jid] = "admission: %s" % (e,)
@@ -333,12 +353,7 @@ class Server:
                 self.graphs = {k: v for k, v in self.graphs.items() if all(i in self.active for i in k)}
                 if not ids:
                     continue
-            g = self._graph_for(ids)
-            t_launch = time.perf_counter()
-            with torch.cuda.stream(self.sample_stream):
-                g.replay()
-                ev = torch.cuda.Event()
-                ev.record(self.sample_stream)
+            ev, t_launch = self._launch(ids)
             self.graph_launches += 1
             for jid in ids:
                 slot = self.active[jid]
