@@ -116,6 +116,29 @@ def test_failure_stays_with_its_job():
     assert rep["jobs"] == 3 and rep["steps"] == 12
 
 
+class LaunchFailServer(HostServer):
+    """The sampling launch of a job whose seed is 7 fails from its third step
+    on (e.g. its graph cannot be captured), alone or together with others."""
+
+    def _launch(self, ids):
+        if any(self.active[i].spec.seed == 7 and self.active[i].steps_done >= 2 for i in ids):
+            raise RuntimeError("capture failed")
+        return super()._launch(ids)
+
+
+def test_failed_launch_stays_with_its_job():
+    srv = LaunchFailServer(hbm_budget=1 << 40, max_slots=4, batch_window=0.0)
+    bad = srv.submit(_spec(steps=5, seed=7))
+    good = [srv.submit(_spec(steps=5, seed=s)) for s in (1, 2, 3)]
+    rep = _run(srv)
+    assert srv.status(bad) == "failed" and "capture failed" in srv.errors[bad]
+    assert srv.done.get(bad) is None and bad not in srv.active
+    assert all(srv.status(i) == "done" for i in good)
+    assert rep["steps"] == 15 and rep["not_completed"] == {bad: "failed"}
+    # after the failure the other jobs were launched on their own
+    assert any(len(k) == 1 for k in srv.launched)
+
+
 def test_cancel_queued_and_active():
     srv = HostServer(hbm_budget=1 << 40, max_slots=2, batch_window=0.0)
 

@@ -20,8 +20,10 @@ x = 1) or a real-time quench (makeReal='imag', x = i), Euler-integrated.
 * Failures stay with their job: an invalid spec is refused at ``submit``, a
   job whose footprint exceeds the whole budget is rejected at admission, a
   job whose step raises (including its ``on_step`` callback) is marked
-  failed, and ``cancel`` withdraws a queued job or stops an active one after
-  its current step; the other jobs continue.  ``status`` reports each job's
+  failed, a shared sampling launch that fails is retried job by job and only
+  the jobs whose own launch fails are marked failed, and ``cancel``
+  withdraws a queued job or stops an active one after its current step; the
+  other jobs continue.  ``status`` reports each job's
   state.
 
 A job computes exactly what it computes alone: its kernels, inputs and
@@ -353,9 +355,13 @@ class Server:
                 self.graphs = {k: v for k, v in self.graphs.items() if all(i in self.active for i in k)}
                 if not ids:
                     continue
-            ev, t_launch = self._launch(ids)
-            self.graph_launches += 1
-            for jid in ids:
+            try:
+                ev, t_launch = self._launch(ids)
+                self.graph_launches += 1
+                batch = [(jid, ev, t_launch) for jid in ids]
+            except Exception:  # find the job(s) whose sampling cannot be launched
+                batch = self._launch_each(ids)
+            for jid, ev, t_launch in batch:
                 slot = self.active[jid]
                 th = threading.Thread(target=self._work, args=(slot, ev, t_launch), daemon=True)
                 workers[jid] = th
@@ -363,6 +369,26 @@ class Server:
         for th in workers.values():
             th.join()
         return self.report()
+
+    def _launch_each(self, ids):
+        """After a shared launch failed: launch each ready job alone.  A job
+        whose own launch fails is marked failed and releases its slot; the
+        others run this step from their own graphs."""
+        batch = []
+        for jid in ids:
+            try:
+                ev, t_launch = self._launch([jid])
+            except Exception as e:
+                with self.lock:
+                    slot = self.active.pop(jid)
+                    slot.job_latency = time.perf_counter() - slot.arrival_wall
+                    self.states[jid] = "failed"
+                    self.errors[jid] = "launch: %s: %s" % (type(e).__name__, e)
+                    self.lock.notify_all()
+                continue
+            self.graph_launches += 1
+            batch.append((jid, ev, t_launch))
+        return batch
 
     def _work(self, slot, ev, t_launch):
         err = None
