@@ -90,7 +90,10 @@ int vmc_exact_probabilities(const double* log_psi, int64_t num_states, int64_t n
 size_t vmc_rbm_tables_bytes(int32_t precision, int32_t num_sites, int32_t num_hidden);
 
 /* Fill the tables: cosh(2W), sinh(2W), exp(2W), exp(-2W), tanh(2W), then
- * sum_j log cosh(2 W_ij) per row i.  Call after every parameter change. */
+ * sum_j log cosh(2 W_ij) per row i.  Call after every parameter change.
+ * No reference counterpart: jVMC re-evaluates rbm.py:29-38 for every s';
+ * these factors let the fused E_loc and Metropolis kernels form the ratios
+ * psi(s')/psi(s) of that same function. */
 int vmc_rbm_prepare(int32_t precision, int32_t num_sites, int32_t num_hidden, const void* kernel, void* tables,
                     vmc_stream_t stream);
 
@@ -124,11 +127,14 @@ int vmc_rbm_metropolis(int32_t precision, int32_t* states, int32_t num_chains, i
                        int64_t samples_per_chain, int32_t* configs_out, void* counters, vmc_stream_t stream);
 
 /* Host-side copy of the Metropolis random stream (no GPU needed): flip sites
- * and acceptance uniforms of `step` for chains 0..num_chains-1 (host arrays). */
+ * and acceptance uniforms of `step` for chains 0..num_chains-1 (host arrays).
+ * Stands where jVMC draws jax.random.randint / bernoulli (sampler.py:15-19,
+ * 330-340); used by tests to replay chains on the host. */
 int vmc_metropolis_draws_host(uint64_t seed, uint32_t call_index, uint32_t step, int32_t num_chains,
                               int32_t num_sites, int32_t* sites, double* uniforms);
 
-/* vmc_rbm_metropolis with the call index read from device memory
+/* vmc_rbm_metropolis (MCSampler._get_samples_mcmc / _sweep, sampler.py:264-367) with
+ * the call index read from device memory
  * (*call_index, uint32) and incremented after the sweep on the same stream:
  * a CUDA graph that captures it draws a fresh random stream on every replay
  * (the serving loop's shared graph launches). */
@@ -143,7 +149,9 @@ int vmc_rbm_metropolis_devcall(int32_t precision, int32_t* states, int32_t num_c
 int vmc_mc_probabilities(const double* log_psi, int64_t num_samples, double factor, double* p, void* workspace,
                          size_t workspace_bytes, vmc_stream_t stream);
 
-/* Vector-Jacobian product of log psi: out_k = sum_n conj(g_n) O_nk (c128, compact
+/* Vector-Jacobian product of log psi (the contraction jax.grad forms inside
+ * NQS.gradients, vqs.py:66-69, 256-287):
+ * out_k = sum_n conj(g_n) O_nk (c128, compact
  * layout) for a cotangent g (N, c128), without materialising O: the
  * activations tanh(theta) are recomputed from the configurations.  The
  * backward of a torch.autograd.Function / jax.custom_vjp over log psi.
@@ -286,7 +294,9 @@ int vmc_rbm_snr_data(int32_t precision, const int32_t* configs, int64_t num_conf
 int vmc_gram_to_hermitian(int32_t gram_precision, const void* gram, int64_t ld_gram, int32_t num_params,
                           double diag_shift, double* A, vmc_stream_t stream);
 
-/* y = U^H x (adjoint = 1) or y = U x (adjoint = 0); U column-major c128.
+/* y = U^H x (adjoint = 1) or y = U x (adjoint = 0); U column-major c128:
+ * VtF = V^dagger F (tdvp.py:171) and update = V (pinv VtF)
+ * (tdvp.py:211).
  * adjoint = 0 needs vmc_zgemv_workspace_bytes(n) of workspace (partial sums
  * over 256-wide chunks of k, added in a fixed order); adjoint = 1 needs none. */
 size_t vmc_zgemv_workspace_bytes(int32_t n);
@@ -336,10 +346,12 @@ int vmc_gemm_bf16x3_colsq(const void* a_hi, const void* a_lo, int32_t m, int64_t
                           size_t workspace_bytes, vmc_stream_t stream);
 
 /* Error flag of the tensor-core kernels (a bounded wait that ran out);
- * synchronises the device.  reset != 0 clears it. */
+ * synchronises the device.  reset != 0 clears it.  No reference
+ * counterpart (XLA reports kernel failures itself). */
 int vmc_tc_error_flag(int32_t reset);
 
-/* B^T planes (2P x 2P, leading dimension ld) of the real representation
+/* Operand of the SNR transform (tdvp.py:175-179): B^T planes (2P x 2P,
+ * leading dimension ld) of the real representation
  * [[Re U, -Im U], [Im U, Re U]] of the eigenvectors U (P x P, column-major
  * c128, leading dimension ldu), split into bf16 hi/lo: the B operand of the
  * SNR contraction. */
