@@ -25,7 +25,7 @@
 #include <cuda.h>
 #include <cuda_bf16.h>
 
-#include <algorithm>
+#include <atomic>
 
 #include "gemm_tiles.cuh"
 #include "vmc_common.cuh"
@@ -285,16 +285,21 @@ typedef CUresult (*encode_fn_t)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, v
                                 const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
+// The driver entry point and the kernel attribute below are set up once per
+// process; host threads of the serving loop call in concurrently.
 static encode_fn_t get_encode() {
-  static encode_fn_t fn = nullptr;
-  if (!fn) {
+  static std::atomic<encode_fn_t> fn{nullptr};
+  encode_fn_t f = fn.load(std::memory_order_acquire);
+  if (!f) {
     void* p = nullptr;
     cudaDriverEntryPointQueryResult q;
     if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q) == cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<encode_fn_t>(p);
+        q == cudaDriverEntryPointSuccess) {
+      f = reinterpret_cast<encode_fn_t>(p);
+      fn.store(f, std::memory_order_release);
+    }
   }
-  return fn;
+  return f;
 }
 
 // 2-D bf16 tensor (rows x cols, cols contiguous, leading dimension ld
@@ -319,12 +324,12 @@ static int make_map(CUtensorMap* m, const void* base, int64_t rows, int64_t cols
 
 static int launch_tc(const CUtensorMap& ah, const CUtensorMap& al, const CUtensorMap& bh, const CUtensorMap& bl,
                      tc_args a, int grid, cudaStream_t st) {
-  static bool attr = false;
-  if (!attr) {
+  static std::atomic<bool> attr{false};
+  if (!attr.load(std::memory_order_acquire)) {
     cudaError_t e = cudaFuncSetAttribute((const void*)tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          TC_SMEM);
     VMC_REQUIRE(e == cudaSuccess, VMC_ERR_CUDA, "tc_gemm: %s", cudaGetErrorString(e));
-    attr = true;
+    attr.store(true, std::memory_order_release);
   }
   tc_gemm_kernel<<<grid, TC_THREADS, TC_SMEM, st>>>(ah, al, bh, bl, a);
   return check_launch("tc_gemm");
