@@ -399,7 +399,7 @@ def kernel_bench(args):
             lo = (x - hi.float()).to(torch.bfloat16)
             del x
             G = torch.empty((rows, rows), dtype=torch.float32, device=dev)
-            fn = lambda: L_.call("vmc_gram_bf16x3", L_.ptr(hi), L_.ptr(lo), rows, K, K, L_.ptr(G), rows, st)
+            fn = lambda: L_.call("vmc_gram_bf16x3", L_.ptr(hi), L_.ptr(lo), rows, K, K, L_.ptr(G), rows, None, st)
             alg = float(rows) * (rows + 1) * K
             hw = 3.0 * rows * rows * K
             shape = {"rows": rows, "k": K}
@@ -413,7 +413,7 @@ def kernel_bench(args):
             cs = torch.empty(n, dtype=torch.float32, device=dev)
             ws = torch.empty(L_.query("vmc_gemm_bf16x3_colsq_workspace_bytes", m, n), dtype=torch.uint8, device=dev)
             fn = lambda: L_.call("vmc_gemm_bf16x3_colsq", L_.ptr(ah), L_.ptr(al), m, K, L_.ptr(bh), L_.ptr(bl), n, K,
-                                 K, L_.ptr(cs), L_.ptr(ws), ws.numel(), st)
+                                 K, L_.ptr(cs), L_.ptr(ws), ws.numel(), None, st)
             alg = 2.0 * m * n * K
             hw = 3.0 * alg
             shape = {"m": m, "n": n, "k": K}

@@ -58,6 +58,26 @@ def test_invalid_arguments_are_rejected_on_the_host():
     assert rc == 5
 
 
+def test_gram_output_alignment_is_checked_on_the_host():
+    """The Gram epilogue stores 16-byte vectors: a leading dimension that is
+    not a multiple of 4 floats, or an output not on 16 bytes, is an argument
+    error, not a launch."""
+    lib = L.load()
+    p = ctypes.c_void_p(4096)
+    rc = lib.vmc_gram_bf16x3(p, p, 130, 64, 64, ctypes.c_void_p(4096), 130, None, None)
+    assert rc == 1 and b"multiple of 4" in lib.vmc_last_error_string()
+    rc = lib.vmc_gram_bf16x3(p, p, 128, 64, 64, ctypes.c_void_p(4100), 128, None, None)
+    assert rc == 1 and b"16 bytes" in lib.vmc_last_error_string()
+
+
+def test_wait_check_arguments_are_checked_on_the_host():
+    lib = L.load()
+    assert lib.vmc_tc_wait_check(1000, None, None) == 1
+    assert lib.vmc_tc_wait_check(0, ctypes.c_void_p(4096), None) == 1
+    assert lib.vmc_tc_wait_check(2_000_000_000, ctypes.c_void_p(4096), None) == 1
+    assert lib.vmc_tc_set_wait_limit(0) == 1
+
+
 def test_symnet_cnn_dense_arguments_are_rejected_on_the_host():
     from vmc_jax_gb300.nets.sym_wrapper import SymDesc
     lib = L.load()

@@ -36,7 +36,7 @@ def test_gram_bf16x3(cuda, rows, k):
     hi, lo = _planes(x, ld)
     ldg = (rows + 15) // 16 * 16
     G = torch.full((rows, ldg), float("nan"), dtype=torch.float32, device=cuda)
-    L.call("vmc_gram_bf16x3", L.ptr(hi), L.ptr(lo), rows, k, ld, L.ptr(G), ldg, L.stream())
+    L.call("vmc_gram_bf16x3", L.ptr(hi), L.ptr(lo), rows, k, ld, L.ptr(G), ldg, None, L.stream())
     torch.cuda.synchronize()
     assert L.query("vmc_tc_error_flag", 1) == 0
     ref = _split_product(hi, lo, hi, lo, k)
@@ -63,10 +63,10 @@ def test_gemm_bf16x3_colsq(cuda, m, n, k):
     colsq = torch.full((n,), float("nan"), dtype=torch.float32, device=cuda)
     ws = torch.empty(L.query("vmc_gemm_bf16x3_colsq_workspace_bytes", m, n), dtype=torch.uint8, device=cuda)
     L.call("vmc_gemm_bf16x3_colsq", L.ptr(ah), L.ptr(al), m, ld, L.ptr(bh), L.ptr(bl), n, ld, k, L.ptr(colsq),
-           L.ptr(ws), ws.numel(), L.stream())
+           L.ptr(ws), ws.numel(), None, L.stream())
     first = colsq.clone()
     L.call("vmc_gemm_bf16x3_colsq", L.ptr(ah), L.ptr(al), m, ld, L.ptr(bh), L.ptr(bl), n, ld, k, L.ptr(colsq),
-           L.ptr(ws), ws.numel(), L.stream())
+           L.ptr(ws), ws.numel(), None, L.stream())
     torch.cuda.synchronize()
     assert torch.equal(first, colsq)  # fixed-order reduction: bitwise reproducible
     assert L.query("vmc_tc_error_flag", 1) == 0
@@ -105,3 +105,27 @@ def test_tdvp_mixed_and_fp32_forms(cuda, precision):
     assert abs(e - e64) / abs(e64) < 1e-6
     assert np.max(np.abs(s - s64)) / np.max(np.abs(s64)) < 1e-4
     assert np.max(np.abs(u - u64)) / np.max(np.abs(u64)) < 5e-2
+
+
+def test_bounded_wait_runs_out_and_reports(cuda):
+    """A wait on a barrier that nothing completes gives up after the limit
+    and writes its code to the caller's status word; the context stays
+    usable (a GEMM right after is exact), and a per-call status word leaves
+    the library-wide flag untouched."""
+    import vmc_jax_gb300._lib as L
+    L.query("vmc_tc_error_flag", 1)
+    status = torch.zeros(1, dtype=torch.int32, device=cuda)
+    L.call("vmc_tc_wait_check", 20_000_000, L.ptr(status), L.stream())
+    torch.cuda.synchronize()
+    assert int(status.item()) == 6
+    assert L.query("vmc_tc_error_flag", 0) == 0
+    x = torch.randn(256, 128, device=cuda)
+    hi, lo = _planes(x, 128)
+    G = torch.full((256, 256), float("nan"), dtype=torch.float32, device=cuda)
+    ok = torch.zeros(1, dtype=torch.int32, device=cuda)
+    L.call("vmc_gram_bf16x3", L.ptr(hi), L.ptr(lo), 256, 128, 128, L.ptr(G), 256, L.ptr(ok), L.stream())
+    torch.cuda.synchronize()
+    assert int(ok.item()) == 0
+    ref = _split_product(hi, lo, hi, lo, 128)
+    iu = torch.triu_indices(256, 256, device=cuda)
+    assert torch.allclose(G.double()[iu[0], iu[1]], ref[iu[0], iu[1]], rtol=0, atol=2e-5 * ref.abs().max().item())

@@ -139,6 +139,32 @@ def test_failed_launch_stays_with_its_job():
     assert any(len(k) == 1 for k in srv.launched)
 
 
+class ReplayFailServer(HostServer):
+    """The replay of any launch that contains the job with seed 9 fails at
+    its second step, after it may have enqueued other jobs' work."""
+
+    def _launch(self, ids):
+        if any(self.active[i].spec.seed == 9 and self.active[i].steps_done == 1 for i in ids):
+            self.launched.append(("replay-failed",) + tuple(ids))
+            raise serving.ReplayError("illegal address")
+        return super()._launch(ids)
+
+
+def test_failed_replay_is_not_run_again():
+    """Jobs of a replay that failed are failed, not re-launched on their own:
+    their chains may already have advanced in this step."""
+    srv = ReplayFailServer(hbm_budget=1 << 40, max_slots=4, batch_window=0.0)
+    bad = srv.submit(_spec(steps=3, seed=9))
+    rep = _run(srv)
+    assert srv.status(bad) == "failed" and "replay" in srv.errors[bad]
+    failed_launch = [k for k in srv.launched if k[0] == "replay-failed"]
+    assert len(failed_launch) == 1
+    # nothing of that launch was retried job by job
+    others = set(failed_launch[0][1:])
+    assert all(srv.status(i) == "failed" for i in others)
+    assert srv.done.get(bad) is None and rep["not_completed"][bad] == "failed"
+
+
 def test_cancel_queued_and_active():
     srv = HostServer(hbm_budget=1 << 40, max_slots=2, batch_window=0.0)
 

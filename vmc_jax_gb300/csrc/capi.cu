@@ -36,6 +36,17 @@ int check_op(const char* fn, const vmc_bf_operator* op, int L) {
   return VMC_OK;
 }
 
+int allow_smem(const void* fn, size_t bytes, const char* what) {
+  if (bytes <= 48 * 1024) return VMC_OK;
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();  // clear the non-sticky error so the next launch is not blamed
+    set_error("%s: cannot allow %zu bytes of dynamic shared memory: %s", what, bytes, cudaGetErrorString(e));
+    return VMC_ERR_CUDA;
+  }
+  return VMC_OK;
+}
+
 }  // namespace vmc
 
 extern "C" int vmc_api_version(void) { return VMC_API_VERSION; }

@@ -284,11 +284,6 @@ static int pick_warps(size_t perWarp, int maxWarps, const char* fn) {
   return w;
 }
 
-template <typename K>
-static void allow_smem(K* fn, size_t bytes) {
-  if (bytes > 48 * 1024) cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-}
-
 // ------------------------------------------------------------ local updates
 // A flip of site q0 changes the outputs of layer l (0-based) only on the
 // square of (l+1)(F-1)+1 sites ending at q0 (output p reads p .. p+F-1), so
@@ -675,12 +670,12 @@ extern "C" int vmc_cnn_logpsi(int32_t precision, const vmc_cnn_desc* desc, const
   if (grid > 152 * 32) grid = 152 * 32;
   cudaStream_t st = as_stream(stream);
   if (precision == VMC_F64) {
-    allow_smem(cnn_logpsi_kernel<double>, smem);
+    VMC_ALLOW_SMEM(cnn_logpsi_kernel<double>, smem, "vmc_cnn_logpsi");
     cnn_logpsi_kernel<double><<<(int)grid, 32 * warps, smem, st>>>(configs, num_configs, g,
                                                                   reinterpret_cast<const double*>(params), warps,
                                                                   reinterpret_cast<double2*>(log_psi));
   } else {
-    allow_smem(cnn_logpsi_kernel<float>, smem);
+    VMC_ALLOW_SMEM(cnn_logpsi_kernel<float>, smem, "vmc_cnn_logpsi");
     cnn_logpsi_kernel<float><<<(int)grid, 32 * warps, smem, st>>>(configs, num_configs, g,
                                                                  reinterpret_cast<const float*>(params), warps,
                                                                  reinterpret_cast<double2*>(log_psi));
@@ -708,12 +703,12 @@ extern "C" int vmc_cnn_gradients(int32_t precision, const vmc_cnn_desc* desc, co
   if (grid > 152 * 32) grid = 152 * 32;
   cudaStream_t st = as_stream(stream);
   if (precision == VMC_F64) {
-    allow_smem(cnn_grad_kernel<double>, smem);
+    VMC_ALLOW_SMEM(cnn_grad_kernel<double>, smem, "vmc_cnn_gradients");
     cnn_grad_kernel<double><<<(int)grid, 32 * warps, smem, st>>>(configs, num_configs, g,
                                                                 reinterpret_cast<const double*>(params), warps,
                                                                 layout, out);
   } else {
-    allow_smem(cnn_grad_kernel<float>, smem);
+    VMC_ALLOW_SMEM(cnn_grad_kernel<float>, smem, "vmc_cnn_gradients");
     cnn_grad_kernel<float><<<(int)grid, 32 * warps, smem, st>>>(configs, num_configs, g,
                                                                reinterpret_cast<const float*>(params), warps, layout,
                                                                out);
@@ -748,12 +743,12 @@ extern "C" int vmc_cnn_metropolis(int32_t precision, const vmc_cnn_desc* desc, i
   cudaStream_t st = as_stream(stream);
   unsigned long long* cnt = reinterpret_cast<unsigned long long*>(counters);
   if (precision == VMC_F64) {
-    allow_smem(cnn_metropolis_local_kernel<double>, smem);
+    VMC_ALLOW_SMEM(cnn_metropolis_local_kernel<double>, smem, "vmc_cnn_metropolis");
     cnn_metropolis_local_kernel<double><<<grid, 32 * warps, smem, st>>>(
         states, num_chains, g, lc, reinterpret_cast<const double*>(params), warps, inSmem, mu, seed, call_index,
         therm_steps, sweep_steps, samples_per_chain, configs_out, cnt);
   } else {
-    allow_smem(cnn_metropolis_local_kernel<float>, smem);
+    VMC_ALLOW_SMEM(cnn_metropolis_local_kernel<float>, smem, "vmc_cnn_metropolis");
     cnn_metropolis_local_kernel<float><<<grid, 32 * warps, smem, st>>>(
         states, num_chains, g, lc, reinterpret_cast<const float*>(params), warps, inSmem, mu, seed, call_index,
         therm_steps, sweep_steps, samples_per_chain, configs_out, cnt);
@@ -789,12 +784,12 @@ extern "C" int vmc_cnn_oloc_fused(int32_t precision, const vmc_cnn_desc* desc, c
   if (grid > 152 * 32) grid = 152 * 32;
   cudaStream_t st = as_stream(stream);
   if (precision == VMC_F64) {
-    allow_smem(cnn_oloc_fused_kernel<double>, smem);
+    VMC_ALLOW_SMEM(cnn_oloc_fused_kernel<double>, smem, "vmc_cnn_oloc_fused");
     cnn_oloc_fused_kernel<double><<<(int)grid, 32 * warps, smem, st>>>(
         configs, num_configs, g, lc, reinterpret_cast<const double*>(params), warps, inSmem, *op,
         reinterpret_cast<const double2*>(log_psi_s), reinterpret_cast<double2*>(oloc));
   } else {
-    allow_smem(cnn_oloc_fused_kernel<float>, smem);
+    VMC_ALLOW_SMEM(cnn_oloc_fused_kernel<float>, smem, "vmc_cnn_oloc_fused");
     cnn_oloc_fused_kernel<float><<<(int)grid, 32 * warps, smem, st>>>(
         configs, num_configs, g, lc, reinterpret_cast<const float*>(params), warps, inSmem, *op,
         reinterpret_cast<const double2*>(log_psi_s), reinterpret_cast<double2*>(oloc));

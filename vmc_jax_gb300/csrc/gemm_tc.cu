@@ -20,8 +20,13 @@
 // block and the stage feeds 12 MMAs (3 products x 4 slices); 2-stage TMA ->
 // shared memory ring (128-byte swizzle, K-major).  Warp 0: TMA producer;
 // warp 1: TMEM owner and MMA issuer; warps 2-5: epilogue (tcgen05.ld of the
-// 128 x 256 FP32 accumulator).  All mbarrier waits are bounded; a timeout
-// sets vmc_tc_error and the CTA unwinds.
+// 128 x 256 FP32 accumulator).  Every mbarrier wait is bounded by
+// vmc_tc_wait_limit_ns of %globaltimer time (host-settable, 2 s by default);
+// a wait that runs out writes its code to the call's status word (or to the
+// library-wide flag when the caller passed none) and the CTA unwinds.  The
+// unwinding itself first lets every TMA copy and MMA already issued finish
+// (waits bounded by a fixed 2 s, independent of the settable limit), so
+// shared memory and TMEM are never released under asynchronous writes.
 #include <cuda.h>
 #include <cuda_bf16.h>
 
@@ -39,9 +44,10 @@ constexpr int TC_STAGE_BYTES = 2 * TC_A_BYTES + 2 * TC_B_BYTES;  // 96 KB: A hi,
 constexpr int TC_SMEM = TC_STAGES * TC_STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
 constexpr int TC_THREADS = 192;
 constexpr uint32_t TC_TMEM_COLS = 256;
-constexpr unsigned long long TC_WAIT_NS = 2000000000ull;  // every wait gives up after 2 s
+constexpr unsigned long long TC_DRAIN_NS = 2000000000ull;  // waits on work already issued, when unwinding
 
 __device__ int vmc_tc_error = 0;
+__device__ unsigned long long vmc_tc_wait_limit_ns = 2000000000ull;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -61,10 +67,15 @@ __device__ __forceinline__ unsigned long long global_ns() {
   return t;
 }
 
+__device__ __forceinline__ void tc_record(int* status, int code) {
+  atomicExch(status ? status : &vmc_tc_error, code);
+}
+
 // Wait until the barrier's phase with the given parity has completed.
-// Returns false (and records the error) once TC_WAIT_NS of wall-clock time
+// Returns false (and records `code`) once `limit_ns` of wall-clock time
 // (%globaltimer) have passed, however long each try_wait suspends.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int code) {
+__device__ __forceinline__ bool mbar_wait_for(uint32_t bar, uint32_t parity, int code, int* status,
+                                              unsigned long long limit_ns) {
   const unsigned long long t0 = global_ns();
   for (;;) {
     uint32_t ok;
@@ -74,10 +85,14 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int cod
         : "r"(bar), "r"(parity)
         : "memory");
     if (ok) return true;
-    if (global_ns() - t0 > TC_WAIT_NS) break;
+    if (global_ns() - t0 > limit_ns) break;
   }
-  atomicExch(&vmc_tc_error, code);
+  tc_record(status, code);
   return false;
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int code, int* status) {
+  return mbar_wait_for(bar, parity, code, status, vmc_tc_wait_limit_ns);
 }
 
 __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int c0, int c1, uint32_t bar) {
@@ -141,6 +156,7 @@ struct tc_args {
   int tilesM, tilesN;
   float* out;         // mode 0: D (row-major, ld = ldOut); mode 1: partial column sums (tilesM * 4, N)
   int64_t ldOut;
+  int* status;        // receives the code of a wait that ran out (NULL: the library-wide flag)
 };
 
 __global__ void __launch_bounds__(TC_THREADS, 1)
@@ -188,7 +204,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       for (int it = 0; it < iters && ok; ++it) {
         const int s = it % TC_STAGES;
         const uint32_t ph = (uint32_t)(it / TC_STAGES) & 1u;
-        ok = mbar_wait(smem_u32(&bars[TC_STAGES + s]), ph ^ 1u, 1);
+        ok = mbar_wait(smem_u32(&bars[TC_STAGES + s]), ph ^ 1u, 1, a.status);
         if (!ok) break;
         const uint32_t full = smem_u32(&bars[s]);
         mbar_expect_tx(full, TC_STAGE_BYTES);
@@ -203,7 +219,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       if (!ok) {
         // drain: let the copies already issued land before the CTA unwinds
         for (int j = issued > TC_STAGES ? issued - TC_STAGES : 0; j < issued; ++j)
-          mbar_wait(smem_u32(&bars[j % TC_STAGES]), (uint32_t)(j / TC_STAGES) & 1u, 4);
+          mbar_wait_for(smem_u32(&bars[j % TC_STAGES]), (uint32_t)(j / TC_STAGES) & 1u, 4, a.status, TC_DRAIN_NS);
       }
     }
   } else if (warp == 1) {
@@ -212,7 +228,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       for (int it = 0; it < iters && ok; ++it) {
         const int s = it % TC_STAGES;
         const uint32_t ph = (uint32_t)(it / TC_STAGES) & 1u;
-        ok = mbar_wait(smem_u32(&bars[s]), ph, 2);
+        ok = mbar_wait(smem_u32(&bars[s]), ph, 2, a.status);
         if (!ok) break;
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         unsigned char* st = smem + s * TC_STAGE_BYTES;
@@ -238,7 +254,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     // epilogue: warps 2..5 -> TMEM lane quadrant (warp % 4)
     const int q = warp & 3;
     const int row = q * 32 + lane;
-    ok = mbar_wait(smem_u32(&bars[2 * TC_STAGES]), 0u, 3);
+    ok = mbar_wait(smem_u32(&bars[2 * TC_STAGES]), 0u, 3, a.status);
     if (ok) {
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const int gr = tm * TC_BM + row;
@@ -272,6 +288,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       }
     }
   }
+  // before TMEM is released, every MMA issued above must have finished: the
+  // accumulator barrier completes only then (its wait returns at once when
+  // the epilogue already saw it complete)
+  if (warp == 1 && lane == 0) mbar_wait_for(smem_u32(&bars[2 * TC_STAGES]), 0u, 5, a.status, TC_DRAIN_NS);
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   if (warp == 1) {
@@ -280,13 +300,27 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   }
 }
 
+// One thread waits on an mbarrier that nothing ever arrives on, with the
+// given limit: the wait runs out and records code 6 in *status.  Lets the
+// host check the timeout path of the waits above without a stalled GEMM.
+__global__ void tc_wait_check_kernel(unsigned long long limit_ns, int* status) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(smem_u32(&bar), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) mbar_wait_for(smem_u32(&bar), 0u, 6, status, limit_ns);
+}
+
 // ---------------------------------------------------------------- host side
 typedef CUresult (*encode_fn_t)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                 const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
-// The driver entry point and the kernel attribute below are set up once per
-// process; host threads of the serving loop call in concurrently.
+// The driver entry point is looked up once per process (host threads of the
+// serving loop call in concurrently); the kernel's shared-memory attribute
+// is per device and is set on every launch.
 static encode_fn_t get_encode() {
   static std::atomic<encode_fn_t> fn{nullptr};
   encode_fn_t f = fn.load(std::memory_order_acquire);
@@ -324,13 +358,7 @@ static int make_map(CUtensorMap* m, const void* base, int64_t rows, int64_t cols
 
 static int launch_tc(const CUtensorMap& ah, const CUtensorMap& al, const CUtensorMap& bh, const CUtensorMap& bl,
                      tc_args a, int grid, cudaStream_t st) {
-  static std::atomic<bool> attr{false};
-  if (!attr.load(std::memory_order_acquire)) {
-    cudaError_t e = cudaFuncSetAttribute((const void*)tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         TC_SMEM);
-    VMC_REQUIRE(e == cudaSuccess, VMC_ERR_CUDA, "tc_gemm: %s", cudaGetErrorString(e));
-    attr.store(true, std::memory_order_release);
-  }
+  VMC_ALLOW_SMEM(tc_gemm_kernel, TC_SMEM, "tc_gemm");
   tc_gemm_kernel<<<grid, TC_THREADS, TC_SMEM, st>>>(ah, al, bh, bl, a);
   return check_launch("tc_gemm");
 }
@@ -340,9 +368,12 @@ static int launch_tc(const CUtensorMap& ah, const CUtensorMap& al, const CUtenso
 using namespace vmc;
 
 extern "C" int vmc_gram_bf16x3(const void* hi, const void* lo, int32_t rows, int32_t k, int64_t ld, float* gram,
-                               int64_t ld_gram, vmc_stream_t stream) {
+                               int64_t ld_gram, int32_t* status, vmc_stream_t stream) {
   VMC_REQUIRE(hi && lo && gram && rows > 0 && k > 0 && ld_gram >= rows, VMC_ERR_INVALID_ARGUMENT,
               "vmc_gram_bf16x3: bad arguments");
+  VMC_REQUIRE(ld_gram % 4 == 0 && ((uintptr_t)gram & 15) == 0, VMC_ERR_INVALID_ARGUMENT,
+              "vmc_gram_bf16x3: the Gram matrix must start on 16 bytes and ld_gram (%lld) be a multiple of 4",
+              (long long)ld_gram);
   CUtensorMap mh, ml, nh, nl;
   int rc;
   if ((rc = make_map(&mh, hi, rows, k, ld, TC_BM))) return rc;
@@ -358,6 +389,7 @@ extern "C" int vmc_gram_bf16x3(const void* hi, const void* lo, int32_t rows, int
   a.tilesN = (rows + TC_BN - 1) / TC_BN;
   a.out = gram;
   a.ldOut = ld_gram;
+  a.status = status;
   return launch_tc(mh, ml, nh, nl, a, (int)tile_count(0, a.tilesM, a.tilesN), as_stream(stream));
 }
 
@@ -378,7 +410,8 @@ extern "C" size_t vmc_gemm_bf16x3_colsq_workspace_bytes(int32_t m, int32_t n) {
 
 extern "C" int vmc_gemm_bf16x3_colsq(const void* a_hi, const void* a_lo, int32_t m, int64_t lda, const void* b_hi,
                                      const void* b_lo, int32_t n, int64_t ldb, int32_t k, float* colsq,
-                                     void* workspace, size_t workspace_bytes, vmc_stream_t stream) {
+                                     void* workspace, size_t workspace_bytes, int32_t* status,
+                                     vmc_stream_t stream) {
   VMC_REQUIRE(a_hi && a_lo && b_hi && b_lo && colsq && m > 0 && n > 0 && k > 0, VMC_ERR_INVALID_ARGUMENT,
               "vmc_gemm_bf16x3_colsq: bad arguments");
   VMC_REQUIRE(workspace && workspace_bytes >= vmc_gemm_bf16x3_colsq_workspace_bytes(m, n), VMC_ERR_WORKSPACE,
@@ -398,11 +431,27 @@ extern "C" int vmc_gemm_bf16x3_colsq(const void* a_hi, const void* a_lo, int32_t
   a.tilesN = (n + TC_BN - 1) / TC_BN;
   a.out = reinterpret_cast<float*>(workspace);
   a.ldOut = 0;
+  a.status = status;
   int rc2 = launch_tc(ah, al, bh, bl, a, (int)tile_count(1, a.tilesM, a.tilesN), as_stream(stream));
   if (rc2) return rc2;
   colsq_reduce_kernel<<<(n + 255) / 256, 256, 0, as_stream(stream)>>>(reinterpret_cast<const float*>(workspace),
                                                                        a.tilesM * 4, n, colsq);
   return check_launch("vmc_gemm_bf16x3_colsq(reduce)");
+}
+
+extern "C" int vmc_tc_set_wait_limit(uint64_t limit_ns) {
+  VMC_REQUIRE(limit_ns > 0, VMC_ERR_INVALID_ARGUMENT, "vmc_tc_set_wait_limit: the limit must be positive");
+  unsigned long long v = (unsigned long long)limit_ns;
+  cudaError_t e = cudaMemcpyToSymbol(vmc_tc_wait_limit_ns, &v, sizeof(v));
+  VMC_REQUIRE(e == cudaSuccess, VMC_ERR_CUDA, "vmc_tc_set_wait_limit: %s", cudaGetErrorString(e));
+  return VMC_OK;
+}
+
+extern "C" int vmc_tc_wait_check(uint64_t limit_ns, int32_t* status, vmc_stream_t stream) {
+  VMC_REQUIRE(status && limit_ns > 0 && limit_ns <= 1000000000ull, VMC_ERR_INVALID_ARGUMENT,
+              "vmc_tc_wait_check: needs a status word and a limit in (0, 1 s]");
+  tc_wait_check_kernel<<<1, 32, 0, as_stream(stream)>>>((unsigned long long)limit_ns, status);
+  return check_launch("vmc_tc_wait_check");
 }
 
 extern "C" int vmc_tc_error_flag(int32_t reset) {

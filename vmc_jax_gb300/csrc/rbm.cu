@@ -457,11 +457,6 @@ int check_rbm_args(const char* fn, int32_t precision, const int32_t* configs, in
   return VMC_OK;
 }
 
-size_t set_smem(const void* fn, size_t bytes) {
-  if (bytes > 48 * 1024) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-  return bytes;
-}
-
 }  // namespace vmc
 
 using namespace vmc;
@@ -506,12 +501,12 @@ extern "C" int vmc_rbm_logpsi(int32_t precision, const int32_t* configs, int64_t
   int grid = grid_for(num_configs);
   cudaStream_t st = as_stream(stream);
   if (precision == VMC_F64) {
-    set_smem((const void*)rbm_logpsi_kernel<double>, smem);
+    VMC_ALLOW_SMEM(rbm_logpsi_kernel<double>, smem, "vmc_rbm_logpsi");
     rbm_logpsi_kernel<double><<<grid, 32 * kWarpsPerBlock, smem, st>>>(
         configs, num_configs, make_params<double>(kernel, bias, num_sites, num_hidden),
         reinterpret_cast<double2*>(log_psi));
   } else {
-    set_smem((const void*)rbm_logpsi_kernel<float>, smem);
+    VMC_ALLOW_SMEM(rbm_logpsi_kernel<float>, smem, "vmc_rbm_logpsi");
     rbm_logpsi_kernel<float><<<grid, 32 * kWarpsPerBlock, smem, st>>>(
         configs, num_configs, make_params<float>(kernel, bias, num_sites, num_hidden),
         reinterpret_cast<double2*>(log_psi));
@@ -534,12 +529,12 @@ extern "C" int vmc_rbm_gradients(int32_t precision, const int32_t* configs, int6
   int grid = grid_for(num_configs);
   cudaStream_t st = as_stream(stream);
   if (precision == VMC_F64) {
-    set_smem((const void*)rbm_grad_kernel<double>, smem);
+    VMC_ALLOW_SMEM(rbm_grad_kernel<double>, smem, "vmc_rbm_gradients");
     rbm_grad_kernel<double><<<grid, 32 * kWarpsPerBlock, smem, st>>>(
         configs, num_configs, make_params<double>(kernel, bias, num_sites, num_hidden), layout,
         reinterpret_cast<double2*>(out));
   } else {
-    set_smem((const void*)rbm_grad_kernel<float>, smem);
+    VMC_ALLOW_SMEM(rbm_grad_kernel<float>, smem, "vmc_rbm_gradients");
     rbm_grad_kernel<float><<<grid, 32 * kWarpsPerBlock, smem, st>>>(
         configs, num_configs, make_params<float>(kernel, bias, num_sites, num_hidden), layout,
         reinterpret_cast<double2*>(out));
@@ -570,13 +565,13 @@ extern "C" int vmc_rbm_oloc_fused(int32_t precision, const int32_t* configs, int
   int grid = grid_for(num_configs);
   cudaStream_t st = as_stream(stream);
   if (precision == VMC_F64) {
-    set_smem((const void*)rbm_oloc_fused_kernel<double>, smem);
+    VMC_ALLOW_SMEM(rbm_oloc_fused_kernel<double>, smem, "vmc_rbm_oloc_fused");
     rbm_oloc_fused_kernel<double><<<grid, 32 * kWarpsPerBlock, smem, st>>>(
         configs, num_configs, make_params<double>(kernel, bias, num_sites, num_hidden),
         reinterpret_cast<const cpx<double>*>(tables), *op, reinterpret_cast<const double2*>(log_psi_s),
         reinterpret_cast<double2*>(oloc));
   } else {
-    set_smem((const void*)rbm_oloc_fused_kernel<float>, smem);
+    VMC_ALLOW_SMEM(rbm_oloc_fused_kernel<float>, smem, "vmc_rbm_oloc_fused");
     rbm_oloc_fused_kernel<float><<<grid, 32 * kWarpsPerBlock, smem, st>>>(
         configs, num_configs, make_params<float>(kernel, bias, num_sites, num_hidden),
         reinterpret_cast<const cpx<float>*>(tables), *op, reinterpret_cast<const double2*>(log_psi_s),
@@ -615,11 +610,11 @@ extern "C" int vmc_rbm_grad_stats(int32_t precision, const int32_t* configs, int
   VMC_REQUIRE(smem <= 227 * 1024, VMC_ERR_UNSUPPORTED, "vmc_rbm_grad_stats: M=%d too large", num_hidden);
   int grid = grid_for(num_configs);
   if (precision == VMC_F64) {
-    set_smem((const void*)rbm_tanh_kernel<double>, smem);
+    VMC_ALLOW_SMEM(rbm_tanh_kernel<double>, smem, "vmc_rbm_grad_stats");
     rbm_tanh_kernel<double><<<grid, 32 * kWarpsPerBlock, smem, st>>>(
         configs, num_configs, make_params<double>(kernel, bias, num_sites, num_hidden), tanhT);
   } else {
-    set_smem((const void*)rbm_tanh_kernel<float>, smem);
+    VMC_ALLOW_SMEM(rbm_tanh_kernel<float>, smem, "vmc_rbm_grad_stats");
     rbm_tanh_kernel<float><<<grid, 32 * kWarpsPerBlock, smem, st>>>(
         configs, num_configs, make_params<float>(kernel, bias, num_sites, num_hidden), tanhT);
   }
@@ -943,11 +938,11 @@ extern "C" int vmc_rbm_vjp(int32_t precision, const int32_t* configs, int64_t nu
   VMC_REQUIRE(smem <= 227 * 1024, VMC_ERR_UNSUPPORTED, "vmc_rbm_vjp: M=%d too large", num_hidden);
   int grid = grid_for(num_configs);
   if (precision == VMC_F64) {
-    set_smem((const void*)rbm_tanh_kernel<double>, smem);
+    VMC_ALLOW_SMEM(rbm_tanh_kernel<double>, smem, "vmc_rbm_vjp");
     rbm_tanh_kernel<double><<<grid, 32 * kWarpsPerBlock, smem, st>>>(
         configs, num_configs, make_params<double>(kernel, bias, num_sites, num_hidden), tanhT);
   } else {
-    set_smem((const void*)rbm_tanh_kernel<float>, smem);
+    VMC_ALLOW_SMEM(rbm_tanh_kernel<float>, smem, "vmc_rbm_vjp");
     rbm_tanh_kernel<float><<<grid, 32 * kWarpsPerBlock, smem, st>>>(
         configs, num_configs, make_params<float>(kernel, bias, num_sites, num_hidden), tanhT);
   }

@@ -33,6 +33,5 @@ int grid_for(int64_t N);
 int check_rbm_args(const char* fn, int32_t precision, const int32_t* configs, int64_t N, int32_t L, int32_t M,
                    const void* kernel);
 // raise the dynamic shared-memory limit of `fn` when above 48 KB
-size_t set_smem(const void* fn, size_t bytes);
 
 }  // namespace vmc

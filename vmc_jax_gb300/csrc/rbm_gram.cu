@@ -351,13 +351,11 @@ static int launch_data(int32_t precision, const int32_t* configs, const void* ke
   VMC_REQUIRE(grid.y <= 65535, VMC_ERR_UNSUPPORTED, "%s: %lld columns", fn, (long long)P);
   cudaStream_t st = as_stream(stream);
   if (precision == VMC_F64) {
-    if (smem > 48 * 1024)
-      cudaFuncSetAttribute((const void*)rbm_data_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    VMC_ALLOW_SMEM(rbm_data_kernel<double>, smem, fn);
     rbm_data_kernel<double><<<grid, 256, smem, st>>>(configs, reinterpret_cast<const cpx<double>*>(kernel),
                                                     reinterpret_cast<const cpx<double>*>(bias), a);
   } else {
-    if (smem > 48 * 1024)
-      cudaFuncSetAttribute((const void*)rbm_data_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    VMC_ALLOW_SMEM(rbm_data_kernel<float>, smem, fn);
     rbm_data_kernel<float><<<grid, 256, smem, st>>>(configs, reinterpret_cast<const cpx<float>*>(kernel),
                                                    reinterpret_cast<const cpx<float>*>(bias), a);
   }

@@ -718,12 +718,12 @@ extern "C" int vmc_sym_rbm_logpsi(int32_t precision, const int32_t* configs, int
   cudaStream_t st = as_stream(stream);
   const sym_params sp = make_sym(sym);
   if (precision == VMC_F64) {
-    set_smem((const void*)sym_rbm_logpsi_kernel<double>, smem);
+    VMC_ALLOW_SMEM(sym_rbm_logpsi_kernel<double>, smem, "vmc_sym_rbm_logpsi");
     sym_rbm_logpsi_kernel<double><<<sym_grid(num_configs), kSymThreads, smem, st>>>(
         configs, num_configs, make_params<double>(kernel, bias, num_sites, num_hidden), sp,
         reinterpret_cast<double2*>(log_psi));
   } else {
-    set_smem((const void*)sym_rbm_logpsi_kernel<float>, smem);
+    VMC_ALLOW_SMEM(sym_rbm_logpsi_kernel<float>, smem, "vmc_sym_rbm_logpsi");
     sym_rbm_logpsi_kernel<float><<<sym_grid(num_configs), kSymThreads, smem, st>>>(
         configs, num_configs, make_params<float>(kernel, bias, num_sites, num_hidden), sp,
         reinterpret_cast<double2*>(log_psi));
@@ -754,12 +754,12 @@ extern "C" int vmc_sym_rbm_gradients(int32_t precision, const int32_t* configs, 
   cudaStream_t st = as_stream(stream);
   const sym_params sp = make_sym(sym);
   if (precision == VMC_F64) {
-    set_smem((const void*)sym_rbm_grad_kernel<double>, smem);
+    VMC_ALLOW_SMEM(sym_rbm_grad_kernel<double>, smem, "vmc_sym_rbm_gradients");
     sym_rbm_grad_kernel<double><<<sym_grid(num_configs), kSymThreads, smem, st>>>(
         configs, num_configs, make_params<double>(kernel, bias, num_sites, num_hidden), sp, layout, TC,
         reinterpret_cast<double2*>(out));
   } else {
-    set_smem((const void*)sym_rbm_grad_kernel<float>, smem);
+    VMC_ALLOW_SMEM(sym_rbm_grad_kernel<float>, smem, "vmc_sym_rbm_gradients");
     sym_rbm_grad_kernel<float><<<sym_grid(num_configs), kSymThreads, smem, st>>>(
         configs, num_configs, make_params<float>(kernel, bias, num_sites, num_hidden), sp, layout, TC,
         reinterpret_cast<double2*>(out));
@@ -768,23 +768,26 @@ extern "C" int vmc_sym_rbm_gradients(int32_t precision, const int32_t* configs, 
 }
 
 template <typename T, int JPT>
-static void launch_sym_oloc(int grid, size_t smem, cudaStream_t st, const int32_t* configs, int64_t N,
+static int launch_sym_oloc(int grid, size_t smem, cudaStream_t st, const int32_t* configs, int64_t N,
                             rbm_params<T> p, sym_params sp, const void* tables, const vmc_bf_operator* op, int G,
                             const double* lps, double* out) {
-  set_smem((const void*)sym_rbm_oloc_fused_kernel<T, JPT>, smem);
+  VMC_ALLOW_SMEM((sym_rbm_oloc_fused_kernel<T, JPT>), smem, "vmc_sym_rbm_oloc_fused");
   sym_rbm_oloc_fused_kernel<T, JPT><<<grid, kSymThreads, smem, st>>>(
       configs, N, p, sp, reinterpret_cast<const cpx<T>*>(tables), *op, G, reinterpret_cast<const double2*>(lps),
       reinterpret_cast<double2*>(out));
+  return VMC_OK;
 }
 
 template <typename T>
 static int dispatch_sym_oloc(int jpt, int grid, size_t smem, cudaStream_t st, const int32_t* configs, int64_t N,
                              rbm_params<T> p, sym_params sp, const void* tables, const vmc_bf_operator* op, int G,
                              const double* lps, double* out) {
-  if (jpt <= 2) launch_sym_oloc<T, 2>(grid, smem, st, configs, N, p, sp, tables, op, G, lps, out);
-  else if (jpt <= 4) launch_sym_oloc<T, 4>(grid, smem, st, configs, N, p, sp, tables, op, G, lps, out);
-  else if (jpt <= 8) launch_sym_oloc<T, 8>(grid, smem, st, configs, N, p, sp, tables, op, G, lps, out);
-  else launch_sym_oloc<T, 16>(grid, smem, st, configs, N, p, sp, tables, op, G, lps, out);
+  int rc;
+  if (jpt <= 2) rc = launch_sym_oloc<T, 2>(grid, smem, st, configs, N, p, sp, tables, op, G, lps, out);
+  else if (jpt <= 4) rc = launch_sym_oloc<T, 4>(grid, smem, st, configs, N, p, sp, tables, op, G, lps, out);
+  else if (jpt <= 8) rc = launch_sym_oloc<T, 8>(grid, smem, st, configs, N, p, sp, tables, op, G, lps, out);
+  else rc = launch_sym_oloc<T, 16>(grid, smem, st, configs, N, p, sp, tables, op, G, lps, out);
+  if (rc) return rc;
   return check_launch("vmc_sym_rbm_oloc_fused");
 }
 
@@ -829,25 +832,25 @@ extern "C" int vmc_sym_rbm_oloc_fused(int32_t precision, const int32_t* configs,
 }
 
 template <typename T, int JPT>
-static void launch_sym_mc(int C, size_t smem, cudaStream_t st, int32_t* states, rbm_params<T> p, sym_params sp,
+static int launch_sym_mc(int C, size_t smem, cudaStream_t st, int32_t* states, rbm_params<T> p, sym_params sp,
                           const void* tables, double mu, uint64_t seed, uint32_t call, int64_t therm, int64_t sweep,
                           int64_t spc, int G, int32_t* out, void* counters) {
-  set_smem((const void*)sym_rbm_metropolis_kernel<T, JPT>, smem);
+  VMC_ALLOW_SMEM((sym_rbm_metropolis_kernel<T, JPT>), smem, "vmc_sym_rbm_metropolis");
   sym_rbm_metropolis_kernel<T, JPT><<<C, kSymThreads, smem, st>>>(
       states, C, p, sp, reinterpret_cast<const cpx<T>*>(tables), mu, seed, call, therm, sweep, spc, G, out,
       reinterpret_cast<unsigned long long*>(counters));
+  return VMC_OK;
 }
 
 template <typename T>
 static int dispatch_sym_mc(int jpt, int C, size_t smem, cudaStream_t st, int32_t* states, rbm_params<T> p,
                            sym_params sp, const void* tables, double mu, uint64_t seed, uint32_t call, int64_t therm,
                            int64_t sweep, int64_t spc, int G, int32_t* out, void* counters) {
-  if (jpt <= 2) launch_sym_mc<T, 2>(C, smem, st, states, p, sp, tables, mu, seed, call, therm, sweep, spc, G, out, counters);
-  else if (jpt <= 4) launch_sym_mc<T, 4>(C, smem, st, states, p, sp, tables, mu, seed, call, therm, sweep, spc, G, out, counters);
-  else if (jpt <= 8) launch_sym_mc<T, 8>(C, smem, st, states, p, sp, tables, mu, seed, call, therm, sweep, spc, G, out, counters);
-  else if (jpt <= 16) launch_sym_mc<T, 16>(C, smem, st, states, p, sp, tables, mu, seed, call, therm, sweep, spc, G, out, counters);
-  else launch_sym_mc<T, 32>(C, smem, st, states, p, sp, tables, mu, seed, call, therm, sweep, spc, G, out, counters);
-  return VMC_OK;
+  if (jpt <= 2) return launch_sym_mc<T, 2>(C, smem, st, states, p, sp, tables, mu, seed, call, therm, sweep, spc, G, out, counters);
+  if (jpt <= 4) return launch_sym_mc<T, 4>(C, smem, st, states, p, sp, tables, mu, seed, call, therm, sweep, spc, G, out, counters);
+  if (jpt <= 8) return launch_sym_mc<T, 8>(C, smem, st, states, p, sp, tables, mu, seed, call, therm, sweep, spc, G, out, counters);
+  if (jpt <= 16) return launch_sym_mc<T, 16>(C, smem, st, states, p, sp, tables, mu, seed, call, therm, sweep, spc, G, out, counters);
+  return launch_sym_mc<T, 32>(C, smem, st, states, p, sp, tables, mu, seed, call, therm, sweep, spc, G, out, counters);
 }
 
 extern "C" int vmc_sym_rbm_metropolis(int32_t precision, int32_t* states, int32_t num_chains, int32_t num_sites,

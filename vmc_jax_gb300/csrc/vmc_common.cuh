@@ -15,6 +15,17 @@ void set_error(const char* fmt, ...);
 int check_launch(const char* what);
 // Validate a branch-free operator descriptor (host side).
 int check_op(const char* fn, const vmc_bf_operator* op, int L);
+// Allow `bytes` of dynamic shared memory for kernel `fn` on the current
+// device (needed above 48 KB; the attribute is per device, so it is set on
+// every call).  Returns VMC_OK or VMC_ERR_CUDA with the kernel and the size
+// in the error string.
+int allow_smem(const void* fn, size_t bytes, const char* what);
+
+#define VMC_ALLOW_SMEM(fn, bytes, what)                                              \
+  do {                                                                               \
+    int vmc_rc_ = ::vmc::allow_smem((const void*)(fn), (size_t)(bytes), (what));    \
+    if (vmc_rc_) return vmc_rc_;                                                     \
+  } while (0)
 
 #define VMC_REQUIRE(cond, code, ...)      \
   do {                                     \

@@ -23,34 +23,28 @@ communicationTime = 0.
 
 
 def distribute_sampling(numSamples, localDevices=None, numChainsPerDevice=1):
-    """Samples per chain and the global sample count (mpi_wrapper.py:53-95)."""
+    """Samples per chain and the number of samples actually drawn, for one
+    process (the contract of mpi_wrapper.py:53-95 at commSize 1).
+
+    Without a chain count every requested sample is drawn: (numSamples,
+    numSamples).  With C = localDevices * numChainsPerDevice chains each
+    chain draws ceil(numSamples / C) samples, so C * ceil(numSamples / C)
+    samples are drawn in total.  That total is stored in ``globNumSamples``,
+    which the TDVP signal-to-noise ratio uses."""
     global globNumSamples
-    samplesPerProcess = numSamples // commSize
-    if rank < numSamples % commSize:
-        samplesPerProcess += 1
     if localDevices is None:
-        globNumSamples = numSamples
-        return samplesPerProcess, globNumSamples
-    numChainsPerProcess = localDevices * numChainsPerDevice
-
-    def spc(spp):
-        return int((spp + numChainsPerProcess - 1) // numChainsPerProcess)
-
-    a = numSamples % commSize
-    globNumSamples = (a * spc(1 + numSamples // commSize) + (commSize - a) * spc(numSamples // commSize)) \
-        * numChainsPerProcess
-    return spc(samplesPerProcess), globNumSamples
+        globNumSamples = int(numSamples)
+        return int(numSamples), globNumSamples
+    chains = int(localDevices) * int(numChainsPerDevice)
+    perChain = -(-int(numSamples) // chains)
+    globNumSamples = perChain * chains
+    return perChain, globNumSamples
 
 
 def first_sample_id():
-    """mpi_wrapper.py:98-111."""
-    mySamples = globNumSamples // commSize
-    firstSampleId = rank * mySamples
-    if rank < globNumSamples % commSize:
-        firstSampleId += rank
-    else:
-        firstSampleId += globNumSamples % commSize
-    return firstSampleId
+    """Index of this process's first sample in the global sample order
+    (mpi_wrapper.py:98-111); a single process starts at 0."""
+    return 0
 
 
 def _as_tensor(data):

@@ -7,9 +7,6 @@ uploads them to the GPU, and the CUDA kernels of csrc/branch_free.cu and
 csrc/rbm.cu expand them.
 """
 
-import copy
-import functools
-
 import numpy as np
 import torch
 
@@ -23,18 +20,14 @@ opDtype = global_defs.tCpx
 
 class LocalOp(dict):
     """Operator acting on one local Hilbert space (branch_free.py:279-308):
-    keys ``idx``, ``map``, ``matEls``, ``diag`` and optionally ``fermionic``."""
+    keys ``idx``, ``map``, ``matEls``, ``diag`` and optionally ``fermionic``.
+    A product with anything else gives an ``OpStr``."""
 
     def __init__(self, **kwargs):
-        for k in kwargs.keys():
-            self[k] = kwargs[k]
+        super().__init__(**kwargs)
 
     def __mul__(self, other):
-        if isinstance(other, dict):
-            return OpStr(self, LocalOp(**other))
-        if isinstance(other, OpStr):
-            return OpStr(self, *other)
-        return OpStr(self, other)
+        return OpStr(self) * other
 
     def __rmul__(self, other):
         return other * OpStr(self)
@@ -94,61 +87,76 @@ def annihilation(idx):
                    diag=False, fermionic=True)
 
 
-def _id_prefactor(*args, val=1.0, **kwargs):
-    return val
+class Coefficient:
+    """Prefactor of an operator string: the product of its factors, each a
+    number or a function of the operator's arguments (the time, for
+    instance).  Calling it evaluates every factor with the arguments given
+    and multiplies the values, left to right."""
+
+    __slots__ = ("factors",)
+
+    def __init__(self, factors):
+        self.factors = tuple(factors)
+
+    def __call__(self, *args, **kwargs):
+        value = 1.0
+        for f in self.factors:
+            value = value * (f(*args) if callable(f) else f)
+        return value
+
+    def __repr__(self):
+        return "Coefficient%r" % (self.factors,)
 
 
-def _prod_fun(f1, f2, *args, **kwargs):
-    return f1(*args) * f2(*args)
+def _factors_and_ops(x):
+    """Split an operand of the string algebra into (prefactor factors, local
+    operators).  Local operators given as plain dicts become ``LocalOp``."""
+    if isinstance(x, LocalOp):
+        return [], [x]
+    if isinstance(x, dict):
+        return [], [LocalOp(**x)]
+    if isinstance(x, Coefficient):
+        return list(x.factors), []
+    if isinstance(x, tuple):
+        factors, ops = [], []
+        for item in x:
+            f, o = _factors_and_ops(item)
+            factors += f
+            ops += o
+        return factors, ops
+    return [x], []  # a number or a function of the operator arguments
 
 
 class OpStr(tuple):
-    """Operator string: an optional prefactor callable followed by local
-    operators (branch_free.py:203-255).  Numbers become constant callables
-    and several prefactors are multiplied into one."""
+    """Operator string (branch_free.py:203-255), stored as a tuple
+    ``(Coefficient, op_1, ..., op_n)``, or ``(op_1, ..., op_n)`` when it
+    has no prefactor.  Items may be given in any order; all numbers and
+    functions among them are collected into the one leading ``Coefficient``.
+    ``op_1 ... op_n`` act right to left, as in the reference.  A product
+    of strings (or of a string and a local operator, number or function)
+    multiplies the coefficients and concatenates the local operators in
+    the order of the factors."""
 
-    def __new__(cls, *args):
-        factors = []
-        ops = []
-        for o in args:
-            if isinstance(o, (LocalOp, dict)):
-                ops.append(o)
-            elif callable(o):
-                factors.append(o)
-            else:
-                factors.append(functools.partial(_id_prefactor, val=o))
-        while len(factors) > 1:
-            factors[0] = functools.partial(_prod_fun, f1=factors[0], f2=factors.pop())
-        return super().__new__(cls, tuple(factors + ops))
+    def __new__(cls, *items):
+        factors, ops = _factors_and_ops(items)
+        head = (Coefficient(factors),) if factors else ()
+        return super().__new__(cls, head + tuple(ops))
 
     def __mul__(self, other):
-        if not isinstance(other, (tuple, OpStr)):
-            other = OpStr(other)
-        if callable(other[0]):
-            return OpStr(*(other[0] * self), *(other[1:]))
-        return OpStr(*self, *other)
+        return OpStr(self, other)
 
-    def __rmul__(self, a):
-        if isinstance(a, dict):
-            return OpStr(LocalOp(**a), *self)
-        newOp = [copy.deepcopy(o) for o in self]
-        if not callable(a):
-            a = functools.partial(_id_prefactor, val=a)
-        if callable(newOp[0]):
-            newOp[0] = functools.partial(_prod_fun, f1=a, f2=newOp[0])
-        else:
-            newOp = [a] + newOp
-        return OpStr(*tuple(newOp))
+    def __rmul__(self, other):
+        return OpStr(other, self)
 
 
 def scal_opstr(a, op):
-    """Operator string rescaled by the number or function ``a``
-    (branch_free.py:258-276)."""
-    if not isinstance(op, (tuple, OpStr)):
-        raise RuntimeError("Can add prefactors only to OpStr or tuple objects.")
-    if isinstance(op, tuple) and not isinstance(op, OpStr):
-        op = OpStr(*op)
-    return a * op
+    """The operator string ``op`` (an ``OpStr`` or a tuple of local
+    operators) multiplied by ``a``, a number or a function of the operator
+    arguments (branch_free.py:258-276)."""
+    if not isinstance(op, tuple):
+        raise RuntimeError("scal_opstr: the operator must be an OpStr or a tuple of local operators, not %s"
+                           % type(op).__name__)
+    return OpStr(a, op)
 
 
 class BranchFreeOperator(Operator):

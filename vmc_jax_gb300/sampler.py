@@ -2,8 +2,10 @@
 
 ``MCSampler`` runs the Metropolis chains of a CpxRBM in one CUDA kernel
 (one warp per chain, incremental hidden-unit fields, Philox4x32-10 random
-numbers; one block per chain for a symmetrised RBM, a full re-evaluation
-per proposal for a CNN) and keeps the chains on the GPU between calls.  ``ExactSampler``
+numbers; one block per chain for a symmetrised RBM; for a CNN, one warp per
+chain that recomputes only the activations a flip can change, from the
+stored activations of every layer) and keeps the chains on the GPU between
+calls.  ``ExactSampler``
 enumerates the basis and forms the Born weights on the GPU.
 """
 

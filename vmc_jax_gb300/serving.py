@@ -49,6 +49,10 @@ from .util.tdvp import TDVP
 from .vqs import NQS
 
 
+class ReplayError(RuntimeError):
+    """A shared graph replay failed after it may have enqueued work."""
+
+
 @dataclasses.dataclass
 class JobSpec:
     L: int
@@ -265,13 +269,19 @@ class Server:
 
     def _launch(self, ids):
         """Replay the sampling + E_loc graph of the ready jobs ``ids``; returns
-        the event the jobs' solves wait on and the launch time."""
+        the event the jobs' solves wait on and the launch time.  A failure
+        while the graph is captured or built has enqueued nothing and raises
+        as it is; a failure of the replay itself may have enqueued part of the
+        jobs' work and raises ``ReplayError``."""
         g = self._graph_for(ids)
         t_launch = time.perf_counter()
-        with torch.cuda.stream(self.sample_stream):
-            g.replay()
-            ev = torch.cuda.Event()
-            ev.record(self.sample_stream)
+        try:
+            with torch.cuda.stream(self.sample_stream):
+                g.replay()
+                ev = torch.cuda.Event()
+                ev.record(self.sample_stream)
+        except Exception as e:
+            raise ReplayError("%s: %s" % (type(e).__name__, e)) from e
         return ev, t_launch
 
     def _used(self):
@@ -359,7 +369,12 @@ class Server:
                 ev, t_launch = self._launch(ids)
                 self.graph_launches += 1
                 batch = [(jid, ev, t_launch) for jid in ids]
-            except Exception:  # find the job(s) whose sampling cannot be launched
+            except ReplayError as e:
+                # part of the jobs' sampling may already have run: re-running it
+                # would advance their chains twice, so every job of the launch fails
+                self._fail(ids, "replay: %s" % (e,))
+                batch = []
+            except Exception:  # capture failed, nothing was enqueued: find the job(s) at fault
                 batch = self._launch_each(ids)
             for jid, ev, t_launch in batch:
                 slot = self.active[jid]
@@ -378,17 +393,26 @@ class Server:
         for jid in ids:
             try:
                 ev, t_launch = self._launch([jid])
+            except ReplayError as e:
+                self._fail([jid], "replay: %s" % (e,))
+                continue
             except Exception as e:
-                with self.lock:
-                    slot = self.active.pop(jid)
-                    slot.job_latency = time.perf_counter() - slot.arrival_wall
-                    self.states[jid] = "failed"
-                    self.errors[jid] = "launch: %s: %s" % (type(e).__name__, e)
-                    self.lock.notify_all()
+                self._fail([jid], "launch: %s: %s" % (type(e).__name__, e))
                 continue
             self.graph_launches += 1
             batch.append((jid, ev, t_launch))
         return batch
+
+    def _fail(self, ids, why):
+        """Mark the jobs ``ids`` failed and release their slots."""
+        with self.lock:
+            for jid in ids:
+                slot = self.active.pop(jid, None)
+                if slot is not None:
+                    slot.job_latency = time.perf_counter() - slot.arrival_wall
+                self.states[jid] = "failed"
+                self.errors[jid] = why
+            self.lock.notify_all()
 
     def _work(self, slot, ev, t_launch):
         err = None

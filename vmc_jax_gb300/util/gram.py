@@ -13,10 +13,11 @@ def _round_up(x, m):
     return (x + m - 1) // m * m
 
 
-def mixed_hermitian(data, w, okMean, shift):
+def mixed_hermitian(data, w, okMean, shift, status=None):
     """A = <O^dagger O>_c (P x P complex128) from the BF16x3 Gram matrix of the
     real representation of the centred data of ``data`` (a util.sr_data
-    producer)."""
+    producer).  ``status``: device int32 word that a timed-out wait of the
+    tensor-core kernel sets (the caller zeroes and checks it)."""
     dev = data.device
     st = _lib.stream()
     N, P = data.N, data.P
@@ -28,7 +29,7 @@ def mixed_hermitian(data, w, okMean, shift):
     ldg = _round_up(R, 16)
     G = torch.empty((R, ldg), dtype=torch.float32, device=dev)
     TIMER.mark("gram_kernel")
-    _lib.call("vmc_gram_bf16x3", _lib.ptr(hi), _lib.ptr(lo), R, N, ld, _lib.ptr(G), ldg, st)
+    _lib.call("vmc_gram_bf16x3", _lib.ptr(hi), _lib.ptr(lo), R, N, ld, _lib.ptr(G), ldg, _lib.ptr(status), st)
     TIMER.mark("hermitian")
     del hi, lo
     A = torch.empty((P, P), dtype=torch.complex128, device=dev)
@@ -36,8 +37,9 @@ def mixed_hermitian(data, w, okMean, shift):
     return A
 
 
-def mixed_snr_colsq(data, w, okMean, E, emean, f, U, x):
-    """Column sums of |H conj(U)|^2 in the real representation (2P floats)."""
+def mixed_snr_colsq(data, w, okMean, E, emean, f, U, x, status=None):
+    """Column sums of |H conj(U)|^2 in the real representation (2P floats);
+    ``status`` as for ``mixed_hermitian``."""
     dev = data.device
     st = _lib.stream()
     N, P = data.N, data.P
@@ -53,6 +55,6 @@ def mixed_snr_colsq(data, w, okMean, E, emean, f, U, x):
     ws = _lib.Workspace.get(_lib.query("vmc_gemm_bf16x3_colsq_workspace_bytes", N, R))
     TIMER.mark("snr_kernel")
     _lib.call("vmc_gemm_bf16x3_colsq", _lib.ptr(hh), _lib.ptr(hl), N, ld, _lib.ptr(bh), _lib.ptr(bl), R, ld, R,
-              _lib.ptr(colsq), _lib.ptr(ws), ws.numel(), st)
+              _lib.ptr(colsq), _lib.ptr(ws), ws.numel(), _lib.ptr(status), st)
     TIMER.mark("snr_tail")
     return colsq

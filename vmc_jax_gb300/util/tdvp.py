@@ -145,6 +145,7 @@ class TDVP:
         from .sr_data import producer
         dev = configs.device
         st = _lib.stream()
+        status = self._status_word(dev)
         flat = configs.reshape(configs.shape[0] * configs.shape[1], -1)
         w = (p if weights is None else weights).reshape(-1).to(torch.float64).contiguous()
         E = Eloc.reshape(-1).to(torch.complex128).contiguous()
@@ -171,7 +172,7 @@ class TDVP:
         # S = <O^dagger O>_c  (tdvp.py:142)
         shift = float(self.diagonalShift) if (self.diagonalShift > 1e-10 and self.makeRealName != 'imag') else 0.0
         TIMER.mark("s_build")
-        A = self._gram(data, w, okMean, shift)
+        A = self._gram(data, w, okMean, shift, status)
 
         # eigendecomposition (tdvp.py:153-171), FP64 on the GPU
         TIMER.mark("eigh")
@@ -189,7 +190,7 @@ class TDVP:
 
         # SNR (tdvp.py:173-181)
         TIMER.mark("snr")
-        snr = self._snr(data, w, okMean, E, emean, f, U, vtf)
+        snr = self._snr(data, w, okMean, E, emean, f, U, vtf, status)
 
         # regularised pseudo-inverse (tdvp.py:183-213)
         TIMER.mark("solve")
@@ -206,6 +207,8 @@ class TDVP:
         _lib.call("vmc_zgemv", 0, _lib.ptr(U), U.stride(1), P, _lib.ptr(coef), _lib.ptr(z), _lib.ptr(ws), ws.numel(),
                   st)
 
+        self._check_status(status)
+
         # bookkeeping in the reference's 2P layout
         self._A, self._shift, self._z, self._covOE = A, shift, z, covOE
         self._leafSizes = [int(q.numel()) for q in psi.params.values()]
@@ -217,6 +220,23 @@ class TDVP:
         if realParams:
             return z.real.contiguous(), res[0], res[1]
         return self._realrep(psi, z), res[0], res[1]
+
+    def _status_word(self, dev):
+        """Device int32 that a tensor-core kernel of this solver sets when one
+        of its bounded waits runs out; zeroed at the start of every RHS."""
+        word = getattr(self, "_status", None)
+        if word is None or word.device != dev:
+            word = torch.zeros(1, dtype=torch.int32, device=dev)
+            self._status = word
+        else:
+            word.zero_()
+        return word
+
+    def _check_status(self, word):
+        code = int(word.item())
+        if code:
+            raise _lib.VmcError("TDVP: a tensor-core kernel gave up waiting (code %d); its output is incomplete"
+                                % code)
 
     def S_dot(self, v):
         """S0 v (tdvp.py:215-216) for a flat real vector v in the
@@ -268,10 +288,10 @@ class TDVP:
             start += n
         return torch.cat(parts)
 
-    def _gram(self, data, w, okMean, shift):
+    def _gram(self, data, w, okMean, shift, status=None):
         if self.precision == "mixed":
             from . import gram as _gram
-            return _gram.mixed_hermitian(data, w, okMean, shift)
+            return _gram.mixed_hermitian(data, w, okMean, shift, status)
         fmt, dt = (0, torch.complex128) if self.precision == "fp64" else (1, torch.complex64)
         X = torch.empty((data.N, data.P), dtype=dt, device=data.device)
         data.centered(w, okMean, fmt, X, None, data.P)
@@ -281,7 +301,7 @@ class TDVP:
             A.diagonal().mul_(1.0 + shift)
         return A
 
-    def _snr(self, data, w, okMean, E, emean, f, U, vtf):
+    def _snr(self, data, w, okMean, E, emean, f, U, vtf, status=None):
         dev = data.device
         st = _lib.stream()
         x = complex(self.rhsPrefactor)
@@ -289,7 +309,7 @@ class TDVP:
         snr = torch.empty(P, dtype=torch.float64, device=dev)
         if self.precision == "mixed":
             from . import gram as _gram
-            colsq = _gram.mixed_snr_colsq(data, w, okMean, E, emean, f, U, x)
+            colsq = _gram.mixed_snr_colsq(data, w, okMean, E, emean, f, U, x, status)
             realRep, cprec = 1, _lib.VMC_F32
         else:
             fmt, dt = (0, torch.complex128) if self.precision == "fp64" else (1, torch.complex64)
