@@ -55,6 +55,10 @@ def parse():
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp32", "fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true",
+                    help="skip the FP64 / plain-FP32 comparison on the same samples after the timed region")
+    ap.add_argument("--plain-steps", type=int, default=1,
+                    help="timed steps of the plain-FP32 form (after one warm-up step) for mixed_over_fp32")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--serve", action="store_true",
                     help="serving load: Poisson stream of independent Ising jobs through vmc_jax_gb300.serving")
@@ -156,6 +160,67 @@ def one_step(ctx, theta):
     return new
 
 
+def accuracy_block(ctx):
+    """Relative errors of the mixed and plain-FP32 forms against the FP64
+    form on one common sample: energy and variance of E_loc, S (the complex
+    P x P matrix A, Frobenius norm), F (covar(O, E)), and the update dtheta
+    (l2 norm and largest entry).  Every form runs its own E_loc kernels
+    (FP64 or FP32) and its own S build, eigendecomposition and solve on the
+    same configurations and weights."""
+    import torch
+    V, psi, H, smp = ctx["V"], ctx["psi"], ctx["H"], ctx["sampler"]
+    configs, _, p = smp.sample()
+    keep = psi.precision
+    ref, errs = None, {}
+
+    def rel(a, b):
+        return float(torch.linalg.norm((a - b).reshape(-1)) / torch.linalg.norm(b.reshape(-1)))
+
+    for prec in ("fp64", "mixed", "fp32"):
+        td = V.util.TDVP(smp, makeReal="real", rhsPrefactor=1., pinvCutoff=1e-8, snrTol=2, precision=prec)
+        psi.precision = "fp64" if prec == "fp64" else "fp32"
+        psi._touch()
+        E = V.operator.BranchFreeOperator.get_O_loc_fused(H, configs, psi, None, 0.)
+        u, res, cut = td._complex_rhs(psi, configs, E, p)
+        cur = {"u": u.detach().clone(), "A": td._A, "f": td._covOE.clone(), "E": complex(td.ElocMean),
+               "var": float(td.ElocVar), "cutoff": float(cut), "residual": float(res)}
+        if ref is None:
+            ref = cur
+            continue
+        errs[prec] = {"energy": abs(cur["E"] - ref["E"]) / abs(ref["E"]),
+                      "variance": abs(cur["var"] - ref["var"]) / abs(ref["var"]),
+                      "S": rel(cur["A"], ref["A"]), "F": rel(cur["f"], ref["f"]),
+                      "dtheta": rel(cur["u"], ref["u"]),
+                      "dtheta_max": float((cur["u"] - ref["u"]).abs().max() / ref["u"].abs().max()),
+                      "pinv_cutoff": cur["cutoff"]}
+        if prec == "mixed":
+            errs[prec]["eigensolver"] = td.refineInfo
+        del cur
+        torch.cuda.empty_cache()
+    psi.precision = keep
+    psi._touch()
+    errs["fp64_pinv_cutoff"] = ref["cutoff"]
+    return errs
+
+
+def plain_fp32_steps_per_s(cfg, steps):
+    """Steps/s of the plain-FP32 form (FP32 kernels, cuBLAS complex64 GEMMs,
+    FP64 eigendecomposition by cuSOLVER) on the same workload, CUDA events
+    over ``steps`` steps after one warm-up step."""
+    import torch
+    ctx = build(cfg, "fp32")
+    theta = ctx["psi"].get_parameters()
+    theta = one_step(ctx, theta)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        theta = one_step(ctx, theta)
+    e1.record()
+    torch.cuda.synchronize()
+    return steps / (e0.elapsed_time(e1) / 1000.0)
+
+
 # ------------------------------------------------------------------ clocks
 class ClockSampler:
     """nvidia-smi clock / throttle samples every 200 ms while active."""
@@ -235,11 +300,11 @@ def cpu_step_seconds(cfg, budget_note):
     if cfg["sampler"] == "mc":
         Ns = cfg["chains"] * cfg["per_chain"]
         chain_steps = cfg["chains"] * (cfg["therm"] + cfg["per_chain"]) * L
-        C, sweeps = (64, 1) if sym else (256, 2)
-        mc = O.MCSampler(psi, (L,), 0, numChains=C, numSamples=sweeps * C, thermalizationSweeps=0, sweepSteps=L)
+        C = 64 if sym else cfg["chains"]
+        mc = O.MCSampler(psi, (L,), 0, numChains=C, numSamples=C, thermalizationSweeps=0, sweepSteps=L)
         t0 = time.perf_counter()
-        mc.sample(numSamples=sweeps * C)
-        out["sampling"] = (time.perf_counter() - t0) / (sweeps * C * L) * chain_steps
+        mc.sample(numSamples=C)
+        out["sampling"] = (time.perf_counter() - t0) / (C * L) * chain_steps
     else:
         Ns = 2 ** L
         out["sampling"] = 0.0
@@ -317,9 +382,10 @@ def cpu_sample_desc(cfg):
                 "chains x one sweep, E_loc and gradients of 64 samples, a 4096^2 x 2048 complex GEMM and a 4096^2 "
                 "eigh; extrapolated to one full step" % cfg["L"])
     if cfg["sampler"] == "mc":
-        return ("oracle (numpy FP64 restatement of jVMC) timed on: Metropolis with 256 chains x two sweeps, "
+        return ("oracle (numpy FP64 restatement of jVMC) timed on: Metropolis of all %d chains for one sweep, "
                 "E_loc and gradients of 512 samples, a 4096^2 x 2048 complex GEMM and a 4096^2 eigh; "
-                "extrapolated to one full step (5.24M chain-steps, 16384 samples, 2P = 33280 GEMMs and eigh)")
+                "extrapolated to one full step (5.24M chain-steps, 16384 samples, 2P = 33280 GEMMs and eigh)"
+                % cfg["chains"])
     return "oracle timed on 256 exact-basis samples, a 4096^2 x 2048 complex GEMM and a 4096^2 eigh, extrapolated"
 
 
@@ -346,29 +412,56 @@ def emit(obj):
     print(json.dumps(obj), flush=True)
 
 
+EXTRAPOLATED = {
+    "sampling": "all chains timed for one sweep of L proposals; the step's thermalisation + sampling sweeps are "
+                "that time multiplied by the sweep count (linear work per sweep)",
+    "eloc": "512 samples timed, multiplied by N_s / 512 (linear work per sample)",
+    "gradients": "512 samples timed, multiplied by N_s / 512 (linear work per sample)",
+    "s_build": "complex FP64 GEMM rate measured at 4096^2 x 2048, applied to the step's 8 N_s (2P)^2 flop",
+    "snr": "same GEMM rate applied to the SNR transform's 8 N_s (2P)^2 flop",
+    "eigh": "LAPACK real symmetric eigh timed at n = 4096, scaled by (2P / 4096)^3",
+}
+
+
+def gpu_config(cfg, workload, precision):
+    """The config keys of the GPU arm's line for the same workload."""
+    if cfg.get("net") == "cnn":
+        ns = cfg["chains"] * cfg["per_chain"]
+        P = 656
+    else:
+        ns = cfg["chains"] * cfg["per_chain"] if cfg["sampler"] == "mc" else 2 ** cfg["L"]
+        P = cfg["L"] * cfg["M"] + cfg["M"]
+    return {"workload": workload, "precision": precision, "num_samples": ns, "num_params_complex": P,
+            "l2": "inputs larger than L2 (O_k bf16 planes %.2f GB)" % (8.0 * P * ns / 1e9),
+            "parallelism": "single GPU", **cfg}
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
     cfg = WORKLOADS[args.workload]
-    try:
-        import threadpoolctl  # noqa: F401
-    except Exception:
-        pass
     # one warm-up sample loads BLAS thread pools and pages; further ones only
     # lengthen the run (the CPU path has nothing to compile)
     for _ in range(min(args.warmup, 1)):
         cpu_step_seconds(cfg, "")
-    secs = []
+    secs, walls = [], []
     for _ in range(args.steps):
+        w0 = time.perf_counter()
         t, parts = cpu_step_seconds(cfg, "")
+        walls.append(time.perf_counter() - w0)
         secs.append(t)
     sec = float(np.mean(secs))
     val = 1.0 / sec
     emit({"metric": "TDVP steps/s", "value": val, "unit": "steps/s", "n_gpus": args.gpus, "steps": args.steps,
           "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak",
           "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "impl": "reference",
-          "config": {"workload": args.workload, **cfg}, "warmup_samples_run": min(args.warmup, 1),
+          "config": gpu_config(cfg, args.workload, args.precision), "warmup_samples_run": min(args.warmup, 1),
+          "measured_wall_s_per_step": float(np.mean(walls)),
+          "extrapolated": {"note": "jVMC (JAX) is not installed on the GPU host; the numpy FP64 restatement of its "
+                                   "algorithm is timed on bounded parts of each phase; ms_per_step is the sum of the "
+                                   "phase estimates, measured_wall_s_per_step the time actually spent per step",
+                           "phases": EXTRAPOLATED},
           "cpu_baseline": {"value": val, "unit": "steps/s", "cores": os.cpu_count(), "kind": "port",
                            "sample": cpu_sample_desc(cfg)},
           "e2e": {"value": val, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -709,6 +802,12 @@ def main():
         e2e = {"value": 1.0 / e2e_s, "unit": "steps/s", "h2d_bytes_per_step": host_theta.numel() * 8,
                "d2h_bytes_per_step": host_out.numel() * 8 + 8}
 
+    accuracy, plain = None, None
+    if not args.no_accuracy and args.precision == "mixed" and cfg.get("net") != "cnn":
+        accuracy = accuracy_block(ctx)
+        if args.plain_steps > 0:
+            plain = plain_fp32_steps_per_s(cfg, args.plain_steps)
+
     if rank != 0:
         return
     peaks = {}
@@ -744,17 +843,25 @@ def main():
     out = {"metric": "TDVP steps/s", "value": aggregate_steps_per_s(args.steps, world, ms), "unit": "steps/s",
            "n_gpus": world,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
-           "scaling": "weak", "vs_baseline": None, "dtype": "f32+bf16x3 (FP64 statistics and eigensolve)",
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32+bf16x3 (FP64 statistics and solve; FP64-accurate eigenpairs that carry the solve)",
            "data": "synthetic (seeded lattice and parameters)",
-           "config": {"workload": args.workload, "precision": args.precision, "num_samples": Ns,
-                      "num_params_complex": P, "l2": "inputs larger than L2 (O_k bf16 planes %.2f GB)" % (8.0 * P * Ns / 1e9),
-                      "parallelism": "replicas" if world > 1 else "single GPU", **cfg},
+           "config": {**gpu_config(cfg, args.workload, args.precision),
+                      "parallelism": "replicas" if world > 1 else "single GPU"},
            "energy": energy, "phase_ms": phases, "gram_kernel_ms": gram_ms, "snr_kernel_ms": snr_ms,
            "roofline": roofline, "clocks": clock, "gpu_launches": launches, "e2e": e2e}
+    if getattr(ctx["tdvp"], "refineInfo", None) is not None:
+        out["eigensolver"] = ctx["tdvp"].refineInfo
+    if accuracy is not None:
+        out["accuracy"] = {"vs": "FP64 form (FP64 kernels, S, eigendecomposition and solve) on the same samples",
+                           "relative_errors": accuracy}
+    if plain is not None:
+        out["plain_fp32_steps_per_s"] = plain
+        out["mixed_over_fp32"] = out["value"] / plain
     if not args.no_cpu_baseline and world == 1:
         sec, parts = cpu_step_seconds(cfg, "")
         out["cpu_baseline"] = {"value": 1.0 / sec, "unit": "steps/s", "cores": os.cpu_count(), "kind": "port",
-                               "sample": cpu_sample_desc(cfg), "phase_seconds": parts}
+                               "sample": cpu_sample_desc(cfg), "phase_seconds": parts,
+                               "extrapolated": EXTRAPOLATED}
     emit(out)
 
 

@@ -365,6 +365,49 @@ int vmc_tc_set_wait_limit(uint64_t limit_ns);
  * reference counterpart (failure detection of this library). */
 int vmc_tc_wait_check(uint64_t limit_ns, int32_t* status, vmc_stream_t stream);
 
+/* FP64-accurate complex product on the BF16 tensor cores (Ozaki split):
+ * C = op(A) B (+ C when accumulate != 0), A, B, C complex128 column-major;
+ * trans_a 'C' (67): op(A) = A^H with A k x m; 'N' (78): op(A) = A with A
+ * m x k.  Every operand column is scaled by a power of two and cut into
+ * `slices` (1..8) slices of 7 bits; slice pairs up to level max_level
+ * (<= 2 (slices - 1)) are summed exactly (FP32 tensor-core groups that stay
+ * below 2^24 units, int64 sums).  slices 8, max_level 7 give entries
+ * within ~2^-48 of the row and column scales.  hermitian != 0: the caller
+ * asserts C is Hermitian (m == n); only blocks on or above the diagonal
+ * are computed and the rest mirrored.  k <= 30720.  Workspace from
+ * vmc_zgemm_ozaki_workspace_bytes (256-byte aligned); *status as for the
+ * other tensor-core kernels.  Replaces the O(n^3) products of the
+ * eigendecomposition behind tdvp.py:157 (jnp.linalg.eigh). */
+size_t vmc_zgemm_ozaki_workspace_bytes(int32_t m, int32_t n, int32_t k, int32_t slices);
+int vmc_zgemm_ozaki(int32_t trans_a, int32_t m, int32_t n, int32_t k, const double* A, int64_t lda, const double* B,
+                    int64_t ldb, double* C, int64_t ldc, int32_t hermitian, int32_t accumulate, int32_t slices,
+                    int32_t max_level, void* workspace, size_t workspace_bytes, int32_t* status,
+                    vmc_stream_t stream);
+
+/* Eigendecomposition of the Hermitian S of the TDVP solve (tdvp.py:153-171,
+ * jnp.linalg.eigh), first stage: the complex64 eigendecomposition of A
+ * (n x n complex128, column-major) by cuSOLVER; ev (n, ascending) and V
+ * (n x n complex128, column-major, ldv) receive the FP32 values and vectors
+ * widened.  *info (device int32) is cuSOLVER's status (0: converged). */
+size_t vmc_eigh_fp32_workspace_bytes(int32_t n);
+int vmc_eigh_fp32(int32_t n, const double* A, int64_t lda, double* ev, double* V, int64_t ldv, void* workspace,
+                  size_t workspace_bytes, int32_t* info, vmc_stream_t stream);
+
+/* Second stage: on entry ev, V from vmc_eigh_fp32 for the same A.  The k
+ * eigenpairs of largest eigenvalue become FP64-accurate: power_steps
+ * products X <- A X diag(1/ev) of the top-k vectors, then Rayleigh-Ritz in
+ * FP64 (G = X^H X and H = X^H A X as FP64-accurate Ozaki products, the
+ * k x k problem H c = theta G c by cuSOLVER zhegvd, V_top = X C).  The other
+ * n - k columns of V are made orthogonal to V_top (one Gram-Schmidt pass)
+ * and renormalised; their eigenvalues keep the FP32 values.  n <= 30720.
+ * *info: zhegvd's status; *status as for the tensor-core kernels.  Replaces
+ * the FP64 jnp.linalg.eigh of tdvp.py:157 for the eigenpairs that carry
+ * the regularised solve. */
+size_t vmc_eigh_refine_workspace_bytes(int32_t n, int32_t k);
+int vmc_eigh_refine_top(int32_t n, const double* A, int64_t lda, int32_t k, int32_t power_steps, double* ev,
+                        double* V, int64_t ldv, void* workspace, size_t workspace_bytes, int32_t* status,
+                        int32_t* info, vmc_stream_t stream);
+
 /* Operand of the SNR transform (tdvp.py:175-179): B^T planes (2P x 2P,
  * leading dimension ld) of the real representation
  * [[Re U, -Im U], [Im U, Re U]] of the eigenvectors U (P x P, column-major

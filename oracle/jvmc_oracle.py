@@ -1005,7 +1005,13 @@ class TDVP:
     numpy's LAPACK eigh of the full 2P representation, as in the reference."""
 
     def __init__(self, sampler, snrTol=2, pinvTol=1e-14, pinvCutoff=1e-8, makeReal='imag',
-                 rhsPrefactor=1.j, diagonalShift=0., crossValidation=False, snrMode="reference"):
+                 rhsPrefactor=1.j, diagonalShift=0., crossValidation=False, snrMode="reference",
+                 perturbS=None):
+        # perturbS = (relative size, seed): multiply every entry of S by
+        # 1 + size * e with e a symmetric N(0, 1) matrix before the
+        # eigendecomposition -- a planted roundoff-sized change that measures
+        # how strongly the solve amplifies it (test instrumentation only).
+        self.perturbS = perturbS
         self.sampler = sampler
         self.snrTol = snrTol
         self.pinvTol = pinvTol
@@ -1038,6 +1044,10 @@ class TDVP:
         return S, F
 
     def _transform_to_eigenbasis(self, S, F):  # tdvp.py:153-171
+        if self.perturbS is not None:
+            size, seed = self.perturbS
+            e = np.random.default_rng(seed).normal(size=S.shape)
+            S = S + S * (size * 0.5 * (e + e.T))
         self.ev, self.V = np.linalg.eigh(S)
         self.VtF = np.conj(self.V).T @ F
 

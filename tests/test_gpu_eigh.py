@@ -1,0 +1,134 @@
+"""Two-stage eigensolver of the TDVP solve (vmc_eigh_fp32 + vmc_eigh_refine_top)
+against matrices of known spectrum and against cuSOLVER's FP64 eigh.
+
+The matrix has the structure of the S matrix of the Monte Carlo TDVP step:
+a top block of eigenvalues in [0.05, 1] (the ones that carry the SNR-
+regularised solve), a graded bulk in [1e-10, 3e-5] and a null space.  Bars
+for the refined top block, relative to the largest eigenvalue: eigenvalues
+1e-13, residual ||A v - theta v|| 1e-13, orthonormality 1e-13, orthogonality
+to the remaining columns 1e-13; the remaining columns keep FP32 accuracy
+(orthonormal to 1e-5, eigenvalues to 1e-5 of the largest)."""
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def _matrix(n, top, null, seed, dev):
+    g = torch.Generator(device=dev).manual_seed(seed)
+    Z = torch.randn(n, n, dtype=torch.complex128, device=dev, generator=g)
+    Q, _ = torch.linalg.qr(Z)
+    rng = np.random.default_rng(seed)
+    lam = np.concatenate([np.zeros(null), np.sort(10.0 ** rng.uniform(-10, np.log10(3e-5), n - top - null)),
+                          np.sort(rng.uniform(0.05, 1.0, top))])
+    lam_t = torch.as_tensor(lam, device=dev)
+    A = (Q * lam_t[None, :]) @ Q.conj().T
+    A = 0.5 * (A + A.conj().T)
+    return A.resolve_conj().contiguous(), lam
+
+
+def _two_stage(L, A, k, steps):
+    n = A.shape[0]
+    dev = A.device
+    ev = torch.empty(n, dtype=torch.float64, device=dev)
+    U = torch.empty((n, n), dtype=torch.complex128, device=dev).mT
+    info = torch.zeros(1, dtype=torch.int32, device=dev)
+    ws = torch.empty(L.query("vmc_eigh_fp32_workspace_bytes", n), dtype=torch.uint8, device=dev)
+    L.call("vmc_eigh_fp32", n, L.ptr(A), n, L.ptr(ev), L.ptr(U), U.stride(1), L.ptr(ws), ws.numel(), L.ptr(info),
+           L.stream())
+    torch.cuda.synchronize()
+    assert int(info.item()) == 0
+    ev32, U32 = ev.clone(), U.clone()
+    status = torch.zeros(1, dtype=torch.int32, device=dev)
+    ws = torch.empty(L.query("vmc_eigh_refine_workspace_bytes", n, k), dtype=torch.uint8, device=dev)
+    L.call("vmc_eigh_refine_top", n, L.ptr(A), n, k, steps, L.ptr(ev), L.ptr(U), U.stride(1), L.ptr(ws), ws.numel(),
+           L.ptr(status), L.ptr(info), L.stream())
+    torch.cuda.synchronize()
+    assert int(info.item()) == 0 and int(status.item()) == 0
+    return ev, U, ev32, U32
+
+
+@pytest.mark.parametrize("n,top,null", [(1536, 200, 40), (2304, 300, 64)])
+def test_refined_top_block(cuda, n, top, null):
+    import vmc_jax_gb300._lib as L
+    A, lam = _matrix(n, top, null, n, cuda)
+    ev, U, ev32, U32 = _two_stage(L, A, top, 4)
+    lmax = lam.max()
+    b = n - top
+    evn = ev.cpu().numpy()
+    assert np.max(np.abs(evn[b:] - lam[b:])) / lmax < 1e-13
+    assert np.max(np.abs(ev32.cpu().numpy() - lam)) / lmax < 1e-5
+    assert np.max(np.abs(evn[:b] - lam[:b])) / lmax < 1e-5
+    Vt = U[:, b:]
+    R = A @ Vt - Vt * ev[b:][None, :]
+    assert (R.abs().max() / lmax).item() < 1e-13
+    eye = torch.eye(top, dtype=torch.complex128, device=cuda)
+    assert (Vt.mH @ Vt - eye).abs().max().item() < 1e-13
+    cross = Vt.mH @ U[:, :b]
+    assert cross.abs().max().item() < 1e-13
+    Vb = U[:, :b]
+    assert (Vb.mH @ Vb - torch.eye(b, dtype=torch.complex128, device=cuda)).abs().max().item() < 1e-5
+    # cuSOLVER FP64 on the same matrix
+    ref, _ = torch.linalg.eigh(A)
+    assert (ev[b:] - ref[b:]).abs().max().item() / lmax < 1e-13
+
+
+def test_refinement_improves_fp32_vectors(cuda):
+    """The FP32 top vectors are ~1e-7 off the exact eigenvectors; after the
+    refinement the projector onto the top block matches the exact one."""
+    import vmc_jax_gb300._lib as L
+    n, top = 1536, 200
+    A, lam = _matrix(n, top, 16, 5, cuda)
+    ev, U, ev32, U32 = _two_stage(L, A, top, 4)
+    ref_ev, ref_U = torch.linalg.eigh(A)
+    b = n - top
+    P_ref = ref_U[:, b:] @ ref_U[:, b:].mH
+    P32 = U32[:, b:] @ U32[:, b:].mH
+    P = U[:, b:] @ U[:, b:].mH
+    e32 = (P32 - P_ref).abs().max().item()
+    e = (P - P_ref).abs().max().item()
+    assert e32 > 1e-10 and e < 1e-13, (e32, e)
+
+
+def test_tdvp_two_stage_matches_fp64_eigensolver(cuda):
+    """The mixed TDVP step with the two-stage eigensolver against the same
+    step with cuSOLVER's FP64 eigendecomposition of the same S, on the same
+    Monte Carlo samples (TFIM L=48, h=1, CpxRBM M=64, 4096 samples): the
+    refined block must carry the solve, and the updates agree to 1e-10."""
+    import vmc_jax_gb300 as V
+    from vmc_jax_gb300.util import tdvp as T
+    L_, M = 48, 64
+    rng = np.random.default_rng(0)
+    b = rng.normal(0, 0.01, M) + 1j * rng.normal(0, 0.01, M)
+    W = rng.normal(0, 0.01, (L_, M)) + 1j * rng.normal(0, 0.01, (L_, M))
+    psi = V.vqs.NQS(V.nets.CpxRBM(numHidden=M, bias=True), precision="fp32")
+    psi(np.zeros((1, 1, L_), np.int32))
+    psi.set_parameters(np.concatenate([b.real, b.imag, W.real.ravel(), W.imag.ravel()]))
+    H = V.operator.BranchFreeOperator()
+    for l in range(L_):
+        H.add(V.operator.scal_opstr(-1.0, (V.operator.Sz(l), V.operator.Sz((l + 1) % L_))))
+        H.add(V.operator.scal_opstr(-1.0, (V.operator.Sx(l),)))
+    smp = V.sampler.MCSampler(psi, (L_,), 0, updateProposer=V.sampler.propose_spin_flip, numChains=512,
+                              numSamples=4096, thermalizationSweeps=32, sweepSteps=L_)
+    configs, _, p = smp.sample()
+    E = H.get_O_loc_fused(configs, psi, None, 0.)
+    td = V.util.TDVP(smp, makeReal="real", rhsPrefactor=1., pinvCutoff=1e-8, snrTol=2, precision="mixed")
+    u2, r2, c2 = td._complex_rhs(psi, configs, E, p)
+    info = td.refineInfo
+    ev2 = td.ev_c.clone()
+    keep = T.TDVP.TWO_STAGE_MIN_P
+    try:
+        T.TDVP.TWO_STAGE_MIN_P = 1 << 30
+        u1, r1, c1 = td._complex_rhs(psi, configs, E, p)
+    finally:
+        T.TDVP.TWO_STAGE_MIN_P = keep
+    print("refinement plan", info)
+    assert info is not None and info["refined"] is not None
+    k = info["refined"]
+    rel = (torch.linalg.norm(u2 - u1) / torch.linalg.norm(u1)).item()
+    lmax = td.ev_c.abs().max().item()
+    assert (ev2[-k:] - td.ev_c[-k:]).abs().max().item() / lmax < 1e-12
+    assert float(c1) == float(c2)
+    assert rel < 1e-10, rel

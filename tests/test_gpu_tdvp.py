@@ -1,12 +1,14 @@
 """TDVP right-hand side of the CUDA path against the oracle and against the
 reference test-suite's fixtures.
 
-Energy and variance: 1e-10 relative (FP64).  Update dtheta: 1e-10 relative
-where the regularised solve is well conditioned; for the 10-site workload
-with N(0, 0.01^2) weights the solve itself amplifies roundoff -- perturbing S
-by 1e-16 relative moves dtheta by ~1.3e-8 relative in the oracle alone
-(eigenvalues span 4e-11..1.8e-2 and the cutoff loop runs to 1e-8) -- so
-there the bar is 1e-6."""
+Energy and variance: 1e-10 relative (FP64).  Update dtheta: 1e-10 relative,
+or 10x the conditioning floor of the solve where that is larger.  The floor
+is measured, not assumed: the oracle's own update is recomputed with every
+entry of S changed by one unit in the last place (relative 2^-52, two random
+symmetric patterns) and the larger relative change of dtheta is the floor.
+For the 10-site workload with N(0, 0.01^2) weights the floor is ~1e-7
+(eigenvalues span 4e-11..1.8e-2 and the cutoff loop runs to 1e-8), so no
+FP64 implementation can hold 1e-10 there."""
 
 import numpy as np
 import pytest
@@ -45,9 +47,24 @@ def _tfim(V, L, J, h):
     return H
 
 
-@pytest.mark.parametrize("scale,tol", [(0.01, 1e-6), (0.1, 1e-10), (0.3, 1e-10)])
+def _conditioning_floor(opsi, Ho, L, makeReal, rhs, tho):
+    """Largest relative change of the oracle's Euler update when S is
+    perturbed by one ulp (two patterns)."""
+    eso = O.ExactSampler(opsi, L)
+    base = O.Euler(timeStep=0.01).step(0, O.TDVP(eso, makeReal=makeReal, rhsPrefactor=rhs, pinvCutoff=1e-8), tho,
+                                       hamiltonian=Ho, psi=opsi)[0] - tho
+    floor = 0.0
+    for seed in (1, 2):
+        td = O.TDVP(eso, makeReal=makeReal, rhsPrefactor=rhs, pinvCutoff=1e-8, perturbS=(2.0 ** -52, seed))
+        moved = O.Euler(timeStep=0.01).step(0, td, tho, hamiltonian=Ho, psi=opsi)[0] - tho
+        floor = max(floor, _rel(moved, base))
+    opsi.set_parameters(tho)
+    return floor
+
+
+@pytest.mark.parametrize("scale", [0.01, 0.1, 0.3])
 @pytest.mark.parametrize("makeReal,rhs", [("real", 1.0), ("imag", 1.j)])
-def test_exact_euler_step(cuda, scale, tol, makeReal, rhs):
+def test_exact_euler_step(cuda, scale, makeReal, rhs):
     """The 10-site TFIM workload: ExactSampler, FP64, one Euler step of 0.01."""
     import vmc_jax_gb300 as V
     L, M = 10, 20
@@ -65,7 +82,11 @@ def test_exact_euler_step(cuda, scale, tol, makeReal, rhs):
     assert abs(complex(td.ElocMean0) - tdo.ElocMean0) / abs(tdo.ElocMean0) < 1e-10
     assert abs(float(td.ElocVar0) - tdo.ElocVar0) / abs(tdo.ElocVar0) < 1e-10
     dth = (new - th).cpu().numpy()
-    assert _rel(dth, newo - tho) < tol
+    floor = _conditioning_floor(opsi, Ho, L, makeReal, rhs, tho)
+    tol = max(1e-10, 10.0 * floor)
+    err = _rel(dth, newo - tho)
+    print("scale %g %s: dtheta error %.2e, conditioning floor %.2e, bar %.2e" % (scale, makeReal, err, floor, tol))
+    assert err <= tol
     md, mdo = td.get_metadata(), tdo.metaData
     assert _rel(md["spectrum"].cpu().numpy(), mdo["spectrum"]) < 1e-9
     assert abs(float(md["tdvp_residual"]) - mdo["tdvp_residual"]) <= 1e-6 * max(mdo["tdvp_residual"], 1e-12) + 1e-14
@@ -215,3 +236,29 @@ def test_checkpoint_resume_reproduces_the_run(cuda, tmp_path):
     got = steps(psi2, td2, st2, 2)
     for a, b in zip(got, ref):
         assert np.array_equal(a, b)
+
+
+def test_minsr_mixed_tangent_kernel(cuda):
+    """MinSR with the tangent kernel on the tcgen05 BF16x3 Gram kernel: the
+    kernel matrix against the FP64 product of the same samples (2e-5
+    relative to its largest entry, the FP32-accumulation bar of the Gram
+    kernel's own test), and the update against the FP64 MinSR at the same
+    pseudo-inverse tolerance (1e-3: the pseudo-inverse amplifies the S-level
+    error by the spread of the retained eigenvalues, 1e3 here)."""
+    import vmc_jax_gb300 as V
+    from vmc_jax_gb300.util.minsr import tangent_kernel_mixed
+    g = torch.Generator(device=cuda).manual_seed(2)
+    X = (torch.randn(300, 700, dtype=torch.complex64, device=cuda, generator=g) * 0.1)
+    T = tangent_kernel_mixed(X)
+    Xd = X.to(torch.complex128)
+    ref = Xd @ Xd.mH
+    assert ((T - ref).abs().max() / ref.abs().max()).item() < 2e-5
+    psi, opsi = _pair(8, 6, True, 0.2, seed=9)
+    H = _tfim(V, 8, 1.0, 0.9)
+    es = V.sampler.ExactSampler(psi, 8)
+    u64 = V.util.MinSR(es, pinvTol=1e-3)(psi.get_parameters(), 0., psi=psi, hamiltonian=H, intStep=0)
+    psi.precision = "fp32"
+    psi._touch()
+    um = V.util.MinSR(es, pinvTol=1e-3, precision="mixed")(psi.get_parameters(), 0., psi=psi, hamiltonian=H,
+                                                          intStep=0)
+    assert _rel(um.cpu().numpy(), u64.cpu().numpy()) < 1e-3

@@ -164,6 +164,8 @@ def ptr(t):
         return None
     if not t.is_cuda:
         raise VmcError("expected a CUDA tensor, got a tensor on %s" % t.device)
+    if t.is_complex() and t.is_conj():
+        raise VmcError("a tensor with a lazy conjugate bit holds the unconjugated values: call resolve_conj() first")
     return t.data_ptr()
 
 

@@ -73,7 +73,7 @@ def build(force=False, verbose=False, extra_flags=()):
             if log.strip():
                 print(log)
     tmp = LIB + ".tmp"
-    cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs
+    cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcusolver"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stdout + r.stderr))

@@ -31,6 +31,7 @@
 #include <cuda_bf16.h>
 
 #include <atomic>
+#include <cmath>
 
 #include "gemm_tiles.cuh"
 #include "vmc_common.cuh"
@@ -462,4 +463,317 @@ extern "C" int vmc_tc_error_flag(int32_t reset) {
     cudaMemcpyToSymbol(vmc_tc_error, &z, sizeof(int));
   }
   return v;
+}
+
+// ===================================================================
+// FP64-accurate complex products (Ozaki split, tcgen05): kernel in
+// oz_gemm.cuh, operand slicing and output assembly below.
+// ===================================================================
+#include "oz_gemm.cuh"
+#include "oz_host.h"
+
+namespace vmc {
+
+constexpr int OZ_MAX_K2 = 61440;  // keeps the int64 tile sums below 2^63
+
+__host__ __device__ inline int64_t oz_pad(int64_t x, int64_t m) { return (x + m - 1) / m * m; }
+
+// Scale exponent of every operand row m (a column of P, P[k][m] = Z[k sk + m sm]):
+// the smallest e with max_k max(|Re|, |Im|) < 2^e (0 for a zero row).
+// One warp per row when the row is contiguous (sk == 1), else lanes along m.
+__global__ void oz_row_exponent_kernel(const double2* __restrict__ Z, int64_t sk, int64_t sm, int K, int M,
+                                       int* __restrict__ e) {
+  if (sk == 1) {
+    const int warpsPerBlock = blockDim.x >> 5;
+    const int m = blockIdx.x * warpsPerBlock + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (m >= M) return;
+    double mx = 0.0;
+    for (int k = lane; k < K; k += 32) {
+      const double2 v = Z[(int64_t)k + (int64_t)m * sm];
+      mx = fmax(mx, fmax(fabs(v.x), fabs(v.y)));
+    }
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if (lane == 0) {
+      int ex = 0;
+      if (mx > 0.0) frexp(mx, &ex);
+      e[m] = ex;
+    }
+  } else {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= M) return;
+    double mx = 0.0;
+    for (int k = 0; k < K; ++k) {
+      const double2 v = Z[(int64_t)k * sk + (int64_t)m * sm];
+      mx = fmax(mx, fmax(fabs(v.x), fabs(v.y)));
+    }
+    int ex = 0;
+    if (mx > 0.0) frexp(mx, &ex);
+    e[m] = ex;
+  }
+}
+
+// Slices of the operand rows: plane i, row m holds n_i 2^(-7(i+1)) of
+// [Re P[:, m] 2^-e_m | Im P[:, m] 2^-e_m] (columns [0, K) and [K, 2K));
+// with bRole, row rowsHalf + m holds the slices of [Im | -Re].  Rows >= M
+// are written as zeros.  32 x 32 tiles through shared memory so that both
+// the reads (either layout of Z) and the writes are coalesced.
+__global__ void oz_slice_kernel(const double2* __restrict__ Z, int64_t sk, int64_t sm, int conj, int K, int M,
+                                int rowsP, int rowsHalf, int bRole, int slices, int64_t K2p,
+                                const int* __restrict__ e, __nv_bfloat16* __restrict__ planes) {
+  __shared__ double2 tile[32][33];
+  const int k0 = blockIdx.x * 32, m0 = blockIdx.y * 32;
+  const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
+  if (sk == 1) {
+#pragma unroll
+    for (int j = 0; j < 32; j += 8) {
+      const int k = k0 + tx, m = m0 + ty + j;
+      double2 v = make_double2(0.0, 0.0);
+      if (k < K && m < M) v = Z[(int64_t)k + (int64_t)m * sm];
+      tile[tx][ty + j] = v;
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < 32; j += 8) {
+      const int m = m0 + tx, k = k0 + ty + j;
+      double2 v = make_double2(0.0, 0.0);
+      if (k < K && m < M) v = Z[(int64_t)k * sk + (int64_t)m * sm];
+      tile[ty + j][tx] = v;
+    }
+  }
+  __syncthreads();
+  const int64_t planeStride = (int64_t)rowsP * K2p;
+#pragma unroll
+  for (int j = 0; j < 32; j += 8) {
+    const int k = k0 + tx, m = m0 + ty + j;
+    if (k >= K || m >= rowsHalf) continue;
+    double2 v = tile[tx][ty + j];
+    if (conj) v.y = -v.y;
+    const int ex = m < M ? e[m] : 0;
+    double re = ldexp(v.x, -ex), im = ldexp(v.y, -ex);
+    __nv_bfloat16* rowA = planes + (int64_t)m * K2p;
+    __nv_bfloat16* rowB = planes + (int64_t)(rowsHalf + m) * K2p;
+    for (int i = 0; i < slices; ++i) {
+      const double sr = rint(re * 128.0), si = rint(im * 128.0);
+      re = re * 128.0 - sr;
+      im = im * 128.0 - si;
+      const float scale = __int_as_float((127 - OZ_BITS * (i + 1)) << 23);
+      const __nv_bfloat16 br = __float2bfloat16_rn((float)sr * scale), bi = __float2bfloat16_rn((float)si * scale);
+      __nv_bfloat16* pa = rowA + i * planeStride;
+      pa[k] = br;
+      pa[K + k] = bi;
+      if (bRole) {
+        __nv_bfloat16* pb = rowB + i * planeStride;
+        pb[k] = bi;
+        pb[K + k] = __hneg(br);
+      }
+    }
+  }
+}
+
+// Zero the padding columns [2K, K2p) of every row of every plane.
+__global__ void oz_pad_kernel(__nv_bfloat16* planes, int64_t rows, int64_t K2p, int K2) {
+  const int w = (int)(K2p - K2);
+  const int64_t n = rows * w;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = t / w;
+    planes[r * K2p + K2 + (t - r * w)] = __float2bfloat16_rn(0.0f);
+  }
+}
+
+// C (column-major, ldc) = alpha product (+ C), the product read from the
+// kernel's row-major [Re | Im] output; with hermitian, entries of the column
+// blocks left of the diagonal block come from the mirrored entry, conjugated.
+__global__ void oz_finish_kernel(const double* __restrict__ out, int64_t ldo, int M, int N, int Np, int hermitian,
+                                 double2* __restrict__ C, int64_t ldc, int accumulate, double alpha) {
+  __shared__ double2 tile[32][33];
+  const int i0 = blockIdx.x * 32, j0 = blockIdx.y * 32;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const bool mirror = hermitian && (j0 / OZ_BN) < (i0 / OZ_BN);
+  if (!mirror) {
+#pragma unroll
+    for (int r = 0; r < 32; r += 8) {
+      const int i = i0 + ty + r, j = j0 + tx;
+      double2 v = make_double2(0.0, 0.0);
+      if (i < M && j < N) v = make_double2(out[(int64_t)i * ldo + j], out[(int64_t)i * ldo + Np + j]);
+      tile[ty + r][tx] = v;
+    }
+  } else {
+#pragma unroll
+    for (int r = 0; r < 32; r += 8) {
+      const int j = j0 + ty + r, i = i0 + tx;
+      double2 v = make_double2(0.0, 0.0);
+      if (i < M && j < N) v = make_double2(out[(int64_t)j * ldo + i], -out[(int64_t)j * ldo + Np + i]);
+      tile[tx][ty + r] = v;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < 32; r += 8) {
+    const int j = j0 + ty + r, i = i0 + tx;
+    if (i < M && j < N) {
+      double2 v = tile[tx][ty + r];
+      v.x *= alpha;
+      v.y *= alpha;
+      double2* dst = C + (int64_t)j * ldc + i;
+      if (accumulate) {
+        const double2 c = *dst;
+        v.x += c.x;
+        v.y += c.y;
+      }
+      *dst = v;
+    }
+  }
+}
+
+size_t oz_operand_bytes(int rows, int K, int slices, bool bRole) {
+  const int64_t half = oz_pad(rows, OZ_BM);
+  const int64_t rowsP = bRole ? 2 * half : half;
+  return (size_t)(slices * rowsP * oz_pad(2 * (int64_t)K, OZ_BK) * 2) + (size_t)oz_pad(half * 4, 256);
+}
+
+int oz_make_operand(void* buf, int rows, int K, int slices, bool bRole, oz_operand& op) {
+  op.rows = rows;
+  op.rowsHalf = (int)oz_pad(rows, OZ_BM);
+  op.rowsP = bRole ? 2 * op.rowsHalf : op.rowsHalf;
+  op.K = K;
+  op.slices = slices;
+  op.K2p = oz_pad(2 * (int64_t)K, OZ_BK);
+  op.planes = reinterpret_cast<__nv_bfloat16*>(buf);
+  op.exps = reinterpret_cast<int*>(reinterpret_cast<char*>(buf) + (size_t)slices * op.rowsP * op.K2p * 2);
+  return VMC_OK;
+}
+
+int oz_slice(const double* Z, int64_t sk, int64_t sm, int conj, oz_operand& op, bool bRole, cudaStream_t st) {
+  const double2* z = reinterpret_cast<const double2*>(Z);
+  if (sk == 1)
+    oz_row_exponent_kernel<<<(op.rows + 7) / 8, 256, 0, st>>>(z, sk, sm, op.K, op.rows, op.exps);
+  else
+    oz_row_exponent_kernel<<<(op.rows + 127) / 128, 128, 0, st>>>(z, sk, sm, op.K, op.rows, op.exps);
+  if (op.rowsHalf > op.rows)
+    cudaMemsetAsync(op.exps + op.rows, 0, (size_t)(op.rowsHalf - op.rows) * sizeof(int), st);
+  dim3 grid((unsigned)((op.K + 31) / 32), (unsigned)(op.rowsHalf / 32));
+  oz_slice_kernel<<<grid, dim3(32, 8), 0, st>>>(z, sk, sm, conj, op.K, op.rows, op.rowsP, op.rowsHalf,
+                                                bRole ? 1 : 0, op.slices, op.K2p, op.exps, op.planes);
+  if (op.K2p > 2 * (int64_t)op.K)
+    oz_pad_kernel<<<1024, 256, 0, st>>>(op.planes, (int64_t)op.slices * op.rowsP, op.K2p, 2 * op.K);
+  return check_launch("oz_slice");
+}
+
+static int make_map_3d(CUtensorMap* m, const void* base, int64_t cols, int64_t rows, int64_t planes) {
+  encode_fn_t enc = get_encode();
+  VMC_REQUIRE(enc, VMC_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
+  VMC_REQUIRE(((uintptr_t)base & 15) == 0 && (cols * 2) % 16 == 0, VMC_ERR_INVALID_ARGUMENT,
+              "sliced operand not 16-byte aligned");
+  cuuint64_t dims[3] = {(cuuint64_t)cols, (cuuint64_t)rows, (cuuint64_t)planes};
+  cuuint64_t strides[2] = {(cuuint64_t)(cols * 2), (cuuint64_t)(cols * rows * 2)};
+  cuuint32_t box[3] = {(cuuint32_t)OZ_BK, (cuuint32_t)OZ_BM, 1};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims, strides, box, estr,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  VMC_REQUIRE(r == CUDA_SUCCESS, VMC_ERR_CUDA, "cuTensorMapEncodeTiled (3-d) failed (%d)", (int)r);
+  return VMC_OK;
+}
+
+static int oz_sms() {
+  int dev = 0, n = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+  return n > 0 ? n : 148;
+}
+
+int oz_multiply(const oz_operand& A, const oz_operand& B, int maxLevel, bool hermitian, double* out, int* status,
+                cudaStream_t st) {
+  VMC_REQUIRE(A.K == B.K && A.K2p == B.K2p, VMC_ERR_INVALID_ARGUMENT, "oz_multiply: reduction lengths differ");
+  VMC_REQUIRE(A.K2p <= OZ_MAX_K2, VMC_ERR_UNSUPPORTED, "oz_multiply: reduction length %d above %d",
+              (int)A.K2p / 2, OZ_MAX_K2 / 2);
+  VMC_REQUIRE(!hermitian || A.rowsHalf == B.rowsHalf, VMC_ERR_INVALID_ARGUMENT,
+              "oz_multiply: a Hermitian product needs a square output");
+  CUtensorMap ma, mb;
+  int rc;
+  if ((rc = make_map_3d(&ma, A.planes, A.K2p, A.rowsP, A.slices))) return rc;
+  if ((rc = make_map_3d(&mb, B.planes, B.K2p, B.rowsP, B.slices))) return rc;
+  oz_args a;
+  a.M = A.rows;
+  a.K2 = (int)A.K2p;
+  a.halfTiles = B.rowsHalf / OZ_BN;
+  a.tilesM = A.rowsHalf / OZ_BM;
+  a.slicesA = A.slices;
+  a.slicesB = B.slices;
+  a.maxLevel = maxLevel;
+  a.hermitian = hermitian ? 1 : 0;
+  a.numTiles = oz_tile_count(a.tilesM, a.halfTiles, a.hermitian);
+  a.lsb = 0;
+  while (1.02 * (double)A.K2p * std::ldexp(1.0, a.lsb + 1) < std::ldexp(1.0, 63)) ++a.lsb;
+  a.ea = A.exps;
+  a.eb = B.exps;
+  a.out = out;
+  a.ldo = 2 * (int64_t)B.rowsHalf;
+  a.status = status;
+  VMC_ALLOW_SMEM(oz_gemm_kernel, OZ_SMEM, "oz_gemm");
+  const int grid = a.numTiles < oz_sms() ? a.numTiles : oz_sms();
+  oz_gemm_kernel<<<grid, OZ_THREADS, OZ_SMEM, st>>>(ma, mb, a);
+  return check_launch("oz_gemm");
+}
+
+int oz_finish(const double* out, const oz_operand& A, const oz_operand& B, bool hermitian, double* C, int64_t ldc,
+              bool accumulate, cudaStream_t st, double alpha) {
+  dim3 grid((unsigned)((A.rows + 31) / 32), (unsigned)((B.rows + 31) / 32));
+  oz_finish_kernel<<<grid, dim3(32, 8), 0, st>>>(out, 2 * (int64_t)B.rowsHalf, A.rows, B.rows, B.rowsHalf,
+                                                  hermitian ? 1 : 0, reinterpret_cast<double2*>(C), ldc,
+                                                  accumulate ? 1 : 0, alpha);
+  return check_launch("oz_finish");
+}
+
+}  // namespace vmc
+
+static size_t zgemm_ozaki_ws(int32_t m, int32_t n, int32_t k, int32_t slices) {
+  return oz_operand_bytes(m, k, slices, false) + oz_operand_bytes(n, k, slices, true) +
+         (size_t)oz_pad(m, OZ_BM) * 2 * (size_t)oz_pad(n, OZ_BN) * 8 + 1024;
+}
+
+extern "C" size_t vmc_zgemm_ozaki_workspace_bytes(int32_t m, int32_t n, int32_t k, int32_t slices) {
+  if (m <= 0 || n <= 0 || k <= 0 || slices < 1 || slices > OZ_MAX_SLICES) return 0;
+  return zgemm_ozaki_ws(m, n, k, slices);
+}
+
+extern "C" int vmc_zgemm_ozaki(int32_t trans_a, int32_t m, int32_t n, int32_t k, const double* A, int64_t lda,
+                               const double* B, int64_t ldb, double* C, int64_t ldc, int32_t hermitian,
+                               int32_t accumulate, int32_t slices, int32_t max_level, void* workspace,
+                               size_t workspace_bytes, int32_t* status, vmc_stream_t stream) {
+  VMC_REQUIRE(trans_a == 'N' || trans_a == 'C', VMC_ERR_INVALID_ARGUMENT,
+              "vmc_zgemm_ozaki: trans_a must be 'N' or 'C'");
+  VMC_REQUIRE(A && B && C && m > 0 && n > 0 && k > 0, VMC_ERR_INVALID_ARGUMENT, "vmc_zgemm_ozaki: bad arguments");
+  VMC_REQUIRE(lda >= (trans_a == 'N' ? m : k) && ldb >= k && ldc >= m, VMC_ERR_INVALID_ARGUMENT,
+              "vmc_zgemm_ozaki: leading dimension too small");
+  VMC_REQUIRE(!hermitian || m == n, VMC_ERR_INVALID_ARGUMENT, "vmc_zgemm_ozaki: a Hermitian product is square");
+  VMC_REQUIRE(slices >= 1 && slices <= OZ_MAX_SLICES && max_level >= 0 && max_level <= 2 * (slices - 1),
+              VMC_ERR_INVALID_ARGUMENT, "vmc_zgemm_ozaki: %d slices, level %d", slices, max_level);
+  VMC_REQUIRE(2 * (int64_t)k <= OZ_MAX_K2, VMC_ERR_UNSUPPORTED, "vmc_zgemm_ozaki: k = %d above %d", k,
+              OZ_MAX_K2 / 2);
+  VMC_REQUIRE(((uintptr_t)A & 15) == 0 && ((uintptr_t)B & 15) == 0 && ((uintptr_t)C & 15) == 0,
+              VMC_ERR_INVALID_ARGUMENT, "vmc_zgemm_ozaki: complex128 arrays must be 16-byte aligned");
+  const size_t need = zgemm_ozaki_ws(m, n, k, slices);
+  VMC_REQUIRE(workspace && workspace_bytes >= need && ((uintptr_t)workspace & 255) == 0, VMC_ERR_WORKSPACE,
+              "vmc_zgemm_ozaki: workspace of %zu bytes (256-byte aligned) needed", need);
+  cudaStream_t st = as_stream(stream);
+  char* ws = reinterpret_cast<char*>(workspace);
+  oz_operand oa, ob;
+  oz_make_operand(ws, m, k, slices, false, oa);
+  ws += oz_operand_bytes(m, k, slices, false);
+  oz_make_operand(ws, n, k, slices, true, ob);
+  ws += oz_operand_bytes(n, k, slices, true);
+  double* out = reinterpret_cast<double*>(ws);
+  int rc;
+  // C = P^H Q with P = op(A)^H: 'C' -> P[kk][mm] = A[kk + mm lda]; 'N' -> P[kk][mm] = conj(A[mm + kk lda])
+  if (trans_a == 'C')
+    rc = oz_slice(A, 1, lda, 0, oa, false, st);
+  else
+    rc = oz_slice(A, lda, 1, 1, oa, false, st);
+  if (rc) return rc;
+  if ((rc = oz_slice(B, 1, ldb, 0, ob, true, st))) return rc;
+  if ((rc = oz_multiply(oa, ob, max_level, hermitian != 0, out, status, st))) return rc;
+  return oz_finish(out, oa, ob, hermitian != 0, C, ldc, accumulate != 0, st, 1.0);
 }

@@ -3,9 +3,12 @@
 update = -O^dagger (O O^dagger)^+ E_loc with the N_s x N_s tangent kernel
 (stats.py:332-336) instead of the P x P matrix S: the cheaper solve when
 N_s < P.  For a CpxRBM the centred, weighted log-derivatives come from the
-CUDA producer (compact P layout), the kernel O O^dagger is one GEMM and the
-pseudo-inverse an FP64 eigendecomposition on the GPU; the holomorphic update
-is returned in the reference's complex 2P form [-w, i w] per leaf
+CUDA producer (compact P layout); the kernel O O^dagger is the tcgen05
+BF16x3 Gram kernel on the real representation of the samples (precision
+"mixed") or one cuBLAS GEMM (FP64 / FP32); the pseudo-inverse is an FP64
+eigendecomposition on the GPU applied as V (inv * (V^dagger e)) (two
+matrix-vector products, no N_s^3 product).  The holomorphic update is
+returned in the reference's complex 2P form [-w, i w] per leaf
 (w = g^dagger T^+ e), which the integrators add to the real parameter vector
 exactly as jVMC does.
 """
@@ -20,21 +23,63 @@ from ..stats import SampledObs
 
 def pinv_hermitian(T, rtol):
     """jnp.linalg.pinv(T, rtol, hermitian=True) (minsr.py:63,74) by eigh:
-    eigenvalues with |l| <= rtol max|l| are dropped."""
+    eigenvalues with |l| <= rtol max|l| are dropped.  Returned factored as
+    (V, inv): T^+ = V diag(inv) V^dagger."""
     ev, V = torch.linalg.eigh(T)
     cut = rtol * torch.max(torch.abs(ev))
     inv = torch.where(torch.abs(ev) > cut, 1.0 / ev, torch.zeros_like(ev))
-    return (V * inv.to(V.dtype)) @ V.mH
+    return V, inv
+
+
+def pinv_apply(factors, x):
+    """T^+ x = V (inv * (V^dagger x)) from the factors of pinv_hermitian."""
+    V, inv = factors
+    x = x.to(V.dtype)
+    return V @ (inv.to(V.dtype) * (V.mH @ x))
+
+
+def tangent_kernel_mixed(X):
+    """X X^dagger (N x N complex128) of complex samples X (N x P) on the
+    tcgen05 Gram kernel: rows [Re X; Im X] as BF16 hi/lo planes, FP32
+    accumulation, assembled in FP64 (the Gram assembly forms sum conj(x_a) x_b
+    over the rows x_a of X, the conjugate of X X^dagger, conjugated back)."""
+    from .gram import _round_up
+    N, P = X.shape
+    dev = X.device
+    ld = _round_up(P, 64)
+    R = 2 * N
+    hi = torch.zeros((R, ld), dtype=torch.bfloat16, device=dev)
+    lo = torch.zeros((R, ld), dtype=torch.bfloat16, device=dev)
+    for half, part in ((0, X.real), (1, X.imag)):
+        x = part.to(torch.float32)
+        h = x.to(torch.bfloat16)
+        hi[half * N:(half + 1) * N, :P] = h
+        lo[half * N:(half + 1) * N, :P] = (x - h.to(torch.float32)).to(torch.bfloat16)
+    ldg = _round_up(R, 16)
+    G = torch.empty((R, ldg), dtype=torch.float32, device=dev)
+    status = torch.zeros(1, dtype=torch.int32, device=dev)
+    st = _lib.stream()
+    _lib.call("vmc_gram_bf16x3", _lib.ptr(hi), _lib.ptr(lo), R, P, ld, _lib.ptr(G), ldg, _lib.ptr(status), st)
+    del hi, lo
+    A = torch.empty((N, N), dtype=torch.complex128, device=dev)
+    _lib.call("vmc_gram_to_hermitian", _lib.VMC_F32, _lib.ptr(G), ldg, N, 0.0, _lib.ptr(A), st)
+    if int(status.item()):
+        raise _lib.VmcError("MinSR: the tangent-kernel Gram kernel gave up waiting (code %d)" % int(status.item()))
+    return torch.conj_physical(A)
 
 
 class MinSR:
     """Energy minimisation via MinSR (arXiv:2302.01941), minsr.py:16-165.
 
     Initializer arguments: ``sampler``, ``pinvTol``, ``diagonalShift``,
-    ``diagonalizeOnDevice`` (must be True), ``precision`` ("fp64" or "fp32":
-    arithmetic of the tangent-kernel GEMM; the pseudo-inverse is FP64)."""
+    ``diagonalizeOnDevice`` (must be True), ``precision`` ("fp64", "fp32" or
+    "mixed": arithmetic of the log-derivative kernels and of the
+    tangent-kernel product -- cuBLAS FP64 / FP32, or the BF16x3 tcgen05 Gram
+    kernel; the pseudo-inverse is FP64 in every case)."""
 
     def __init__(self, sampler, pinvTol=1e-14, diagonalShift=0., diagonalizeOnDevice=True, precision="fp64"):
+        if precision not in ("fp64", "fp32", "mixed"):
+            raise ValueError("precision must be 'fp64', 'fp32' or 'mixed'")
         if not diagonalizeOnDevice:
             raise NotImplementedError("diagonalisation runs on the GPU; there is no host path")
         self.sampler = sampler
@@ -62,13 +107,12 @@ class MinSR:
         e = eloc._data.reshape(-1)
         if holomorphic:
             T = gradients.tangent_kernel()
-            T_inv = pinv_hermitian(T, self.pinvTol)
-            return -(G.conj().T @ (T_inv @ e.to(T_inv.dtype)))
+            v = pinv_apply(pinv_hermitian(T, self.pinvTol), e)
+            return -(G.conj().T @ v.to(G.dtype))
         G = torch.cat([G.real, G.imag], dim=0).to(torch.float64)
         T = G @ G.T + self.diagonalShift * torch.eye(G.shape[0], dtype=G.dtype, device=G.device)
-        T_inv = pinv_hermitian(T, self.pinvTol)
         ee = torch.cat([e.real, e.imag]).to(torch.float64)
-        return -(G.T @ (T_inv @ ee))
+        return -(G.T @ pinv_apply(pinv_hermitian(T, self.pinvTol), ee))
 
     def _rbm_update(self, psi, configs, Eloc, p):
         """The holomorphic MinSR update for a CpxRBM from the CUDA kernels."""
@@ -78,7 +122,7 @@ class MinSR:
         N, L = flat.shape
         w = p.reshape(-1).to(torch.float64).contiguous()
         E = Eloc.reshape(-1).to(torch.complex128).contiguous()
-        kp = "fp64" if self.precision == "fp64" else "fp32"
+        kp = "fp64" if self.precision == "fp64" else "fp32"  # "mixed": FP32 kernels
         params = psi.params_for(kp)
         prec = CpxRBM._prec(kp)
         M = int(params["kernel"].shape[1])
@@ -99,10 +143,12 @@ class MinSR:
         _lib.call("vmc_rbm_centered_gradients", prec, _lib.ptr(flat), N, L, M, Wk, bk, _lib.ptr(w),
                   _lib.ptr(okMean), fmt, _lib.ptr(X), None, P, st)
         # reference 2P data [g, i g] per leaf: its tangent kernel is 2 g g^dagger
-        T = (2.0 * (X @ X.mH)).to(torch.complex128)
-        T_inv = pinv_hermitian(T, self.pinvTol)
+        if self.precision == "mixed":
+            T = 2.0 * tangent_kernel_mixed(X)
+        else:
+            T = (2.0 * (X @ X.mH)).to(torch.complex128)
         e = torch.sqrt(w).to(torch.complex128) * (E - emean[0])
-        v = T_inv @ e
+        v = pinv_apply(pinv_hermitian(T, self.pinvTol), e)
         wv = X.to(torch.complex128).mH @ v     # g^dagger T^+ e  (P)
         parts, start = [], 0
         for name, prm in psi.params.items():

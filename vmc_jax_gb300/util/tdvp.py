@@ -18,7 +18,10 @@ of the complex P x P matrix A = <O^dagger O>_c; its spectrum is that of A
 with every eigenvalue paired ({l, l} for makeReal='real', {l, -l} for
 'imag'), and the update solves A z = -x covar(O, E) with the same
 regulariser, returned as [Re z; Im z] per leaf.  The eigendecomposition is
-therefore done on the P x P complex matrix (cuSOLVER, FP64).
+therefore done on the P x P complex matrix: cuSOLVER FP64, or, in the mixed
+form with Monte Carlo samples, FP32 cuSOLVER followed by FP64-accurate
+Rayleigh-Ritz refinement of the eigenpairs that carry the solve
+(csrc/eigh.cu).
 
 SNR: for makeReal='imag' the SNR of a pair is unique and identical to the
 reference's; for makeReal='real' the reference's eigenvectors within a
@@ -55,6 +58,80 @@ def transform_helper(x, rhsPrefactor, makeReal):
     return makeReal((-rhsPrefactor) * x)
 
 
+REFINE_EXCLUDED_NORM = 1e-12   # weight the FP32-only eigenpairs may carry, relative
+REFINE_CARRY = 1e-6            # components above this fraction of the largest weight carry the solve
+REFINE_MAX_FRACTION = 1.0 / 3  # refine at most this fraction of the spectrum
+REFINE_MAX_RHO = 0.25          # largest |lambda_excluded / lambda_carrying| accepted
+REFINE_GAP_WINDOW = 1.0 / 8    # search window (fraction of n) for the spectral gap below them
+
+
+def solve_weights(ev, vtf, snr, pinvCutoff, snrTol, snrMargin=1.0):
+    """Upper bound of every eigenpair's share |pinv_k (U^H f)_k| of the
+    update (tdvp.py:195-211): the regulariser at the smallest cutoff the
+    loop can reach, the SNR scaled by snrMargin."""
+    lmax = np.max(np.abs(ev))
+    r = np.abs(ev) / lmax if lmax > 0 else np.zeros_like(ev)
+    with np.errstate(divide="ignore", over="ignore", invalid="ignore"):
+        regc = np.where(r > 0, 1.0 / (1.0 + (pinvCutoff / r) ** 6), 0.0)
+        regs = 1.0 / (1.0 + (snrTol / (snrMargin * np.maximum(snr, 1e-300))) ** 6)
+        inv = np.where(r > 1e-14, 1.0 / np.maximum(np.abs(ev), 1e-300), 0.0)
+    return inv * regc * regs * np.abs(vtf)
+
+
+def refine_plan(ev, vtf, snr, pinvCutoff, snrTol):
+    """Number k of top eigenpairs to refine to FP64 accuracy and the power
+    steps q, from the FP32 eigendecomposition (ev ascending, vtf = U^H f,
+    snr); None when the FP64 eigensolver of the whole matrix is to be used.
+
+    The components that carry the update (weight >= REFINE_CARRY of the
+    largest, weights from solve_weights) are read off the FP32 values,
+    which are accurate for them.  The split b is the largest relative gap
+    |lambda_b / lambda_(b-1)| of the spectrum at or below the lowest carrying
+    component, within REFINE_GAP_WINDOW n of it.  The FP32 bulk vectors are
+    not used to judge the bulk: their projections carry a ~1e-6 share of the
+    top block (FP32 rotation between the blocks) that inflates their SNR;
+    the bulk's share is checked after the refinement (bulk_weight).  Per
+    power step the FP32 error of a carrying component (~1e-7 lambda_max /
+    gap) shrinks by rho = |lambda_(b-1)| / |lambda_carrying min|."""
+    n = ev.shape[0]
+    lmax = np.max(np.abs(ev))
+    if lmax == 0.0:
+        return None
+    c = solve_weights(ev, vtf, snr, pinvCutoff, snrTol)
+    if not np.all(np.isfinite(c)) or c.max() == 0.0:
+        return None
+    j = int(np.nonzero(c >= REFINE_CARRY * c.max())[0].min())
+    if j < 1:
+        return None
+    lo = max(1, j - int(REFINE_GAP_WINDOW * n))
+    a = np.abs(ev)
+    cand = np.arange(lo, j + 1)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        ratio = a[cand] / np.maximum(a[cand - 1], 1e-300 * lmax)
+    b = int(cand[int(np.argmax(ratio))])
+    k = n - b
+    if k > REFINE_MAX_FRACTION * n:
+        return None
+    rho = a[b - 1] / a[j]
+    if not rho < REFINE_MAX_RHO:
+        return None
+    gap = max(a[j] - a[b - 1], 1e-300)
+    eps0 = min(1.0, 1e-7 * lmax / gap)
+    q = 0 if rho == 0.0 else int(np.ceil(np.log(1e-16 / eps0) / np.log(rho)))
+    return k, int(min(max(q, 1), 16))
+
+
+def bulk_weight(ev, vtf, snr, k, pinvCutoff, snrTol):
+    """Share of the update carried by the n - k eigenpairs left at FP32
+    accuracy, from the values after the refinement (the bulk vectors are then
+    orthogonal to the refined block, so their projections are free of its
+    share); the solve falls back to the FP64 eigensolver above
+    REFINE_EXCLUDED_NORM."""
+    c = solve_weights(ev, vtf, snr, pinvCutoff, snrTol)
+    tot = np.sqrt(np.sum(c * c))
+    return float(np.sqrt(np.sum(c[:len(c) - k] ** 2)) / tot) if tot > 0 else 0.0
+
+
 class TDVP:
     """Solver of the TDVP equation  q[S] theta_dot = -q[x F]  by regularised
     pseudo-inverse (tdvp.py:26-94).
@@ -68,8 +145,12 @@ class TDVP:
           ``"fp64"`` (the reference's), ``"fp32"`` (plain FP32 GPU form:
           FP32 kernels, FP32 complex GEMMs) or ``"mixed"`` (FP32 kernels,
           S and the SNR contraction in BF16 with hi/lo split correction and
-          FP32 accumulation on tcgen05).  Means, variances and the
-          eigendecomposition / solve are FP64 in every mode.
+          FP32 accumulation on tcgen05).  Means, variances and the solve are
+          FP64 in every mode; the eigendecomposition is cuSOLVER's FP64 one,
+          except in the mixed form with Monte Carlo samples, where the
+          eigenpairs that carry the SNR-regularised solve are made
+          FP64-accurate on the tensor cores from an FP32 eigendecomposition
+          (util/tdvp.py refine_plan; the rest keep FP32 eigenvalues).
     """
 
     def __init__(self, sampler, snrTol=2, pinvTol=1e-14, pinvCutoff=1e-8, makeReal='imag', rhsPrefactor=1.j,
@@ -174,29 +255,55 @@ class TDVP:
         TIMER.mark("s_build")
         A = self._gram(data, w, okMean, shift, status)
 
-        # eigendecomposition (tdvp.py:153-171), FP64 on the GPU
+        # eigendecomposition (tdvp.py:153-171) and SNR (tdvp.py:173-181)
         TIMER.mark("eigh")
-        if realParams:  # S real symmetric: the real eigensolver, vectors as complex
-            ev, U = torch.linalg.eigh(A.real.contiguous())
-            U = U.to(torch.complex128)
+        self.refineInfo = None
+        useSnr = not isinstance(self.sampler, ExactSampler)
+        if self._two_stage(realParams, useSnr, P):
+            ev, U = self._eigh_fp32(A)
+            vtf = self._project(U, f)
+            TIMER.mark("snr")
+            snr = self._snr(data, w, okMean, E, emean, f, U, vtf, status)
+            plan = refine_plan(ev.cpu().numpy(), vtf.cpu().numpy(), snr.cpu().numpy(), self.pinvCutoff,
+                               self.snrTol)
+            weight = None
+            if plan is not None:
+                TIMER.mark("eigh")
+                self._eigh_refine(A, ev, U, plan[0], plan[1], status)
+                vtf = self._project(U, f)
+                TIMER.mark("snr")
+                snr = self._snr(data, w, okMean, E, emean, f, U, vtf, status)
+                weight = bulk_weight(ev.cpu().numpy(), vtf.cpu().numpy(), snr.cpu().numpy(), plan[0],
+                                     self.pinvCutoff, self.snrTol)
+                if weight > REFINE_EXCLUDED_NORM:
+                    plan = None
+            if plan is None:
+                TIMER.mark("eigh")
+                ev, U = torch.linalg.eigh(A)
+                if U.stride(0) != 1:
+                    U = U.mT.contiguous().mT
+                vtf = self._project(U, f)
+                TIMER.mark("snr")
+                snr = self._snr(data, w, okMean, E, emean, f, U, vtf, status)
+            self.refineInfo = {"refined": None if plan is None else plan[0],
+                               "power_steps": None if plan is None else plan[1], "n": P,
+                               "fp32_bulk_weight": weight}
         else:
-            ev, U = torch.linalg.eigh(A)
-        if U.stride(0) != 1:
-            U = U.mT.contiguous().mT
-        vtf = torch.empty(P, dtype=torch.complex128, device=dev)
-        ws = _lib.Workspace.get(_lib.query("vmc_zgemv_workspace_bytes", P))
-        _lib.call("vmc_zgemv", 1, _lib.ptr(U), U.stride(1), P, _lib.ptr(f), _lib.ptr(vtf), _lib.ptr(ws), ws.numel(),
-                  st)
-
-        # SNR (tdvp.py:173-181)
-        TIMER.mark("snr")
-        snr = self._snr(data, w, okMean, E, emean, f, U, vtf, status)
+            if realParams:  # S real symmetric: the real eigensolver, vectors as complex
+                ev, U = torch.linalg.eigh(A.real.contiguous())
+                U = U.to(torch.complex128)
+            else:
+                ev, U = torch.linalg.eigh(A)
+            if U.stride(0) != 1:
+                U = U.mT.contiguous().mT
+            vtf = self._project(U, f)
+            TIMER.mark("snr")
+            snr = self._snr(data, w, okMean, E, emean, f, U, vtf, status)
 
         # regularised pseudo-inverse (tdvp.py:183-213)
         TIMER.mark("solve")
         pinv = torch.empty(P, dtype=torch.float64, device=dev)
         res = torch.empty(3, dtype=torch.float64, device=dev)
-        useSnr = not isinstance(self.sampler, ExactSampler)
         ws = _lib.Workspace.get(_lib.query("vmc_tdvp_regularize_workspace_bytes", P, float(self.pinvCutoff)))
         _lib.call("vmc_tdvp_regularize", _lib.ptr(ev), _lib.ptr(vtf), _lib.ptr(snr) if useSnr else None, P,
                   float(self.pinvCutoff), float(self.pinvTol), float(self.snrTol), _lib.ptr(pinv), _lib.ptr(res),
@@ -220,6 +327,49 @@ class TDVP:
         if realParams:
             return z.real.contiguous(), res[0], res[1]
         return self._realrep(psi, z), res[0], res[1]
+
+    # ------------------------------------------- eigendecomposition stages
+    TWO_STAGE_MIN_P = 2048
+
+    def _two_stage(self, realParams, useSnr, P):
+        """The mixed form with Monte Carlo samples solves through the two-stage
+        eigensolver (FP32 eigendecomposition, then the eigenpairs that carry
+        the SNR-regularised solve refined to FP64 accuracy on the tensor
+        cores); every other case through the FP64 cuSOLVER eigensolver."""
+        return self.precision == "mixed" and useSnr and not realParams and P >= self.TWO_STAGE_MIN_P
+
+    def _project(self, U, f):
+        """U^H f (FP64, fixed-order reduction)."""
+        P = U.shape[0]
+        vtf = torch.empty(P, dtype=torch.complex128, device=U.device)
+        ws = _lib.Workspace.get(_lib.query("vmc_zgemv_workspace_bytes", P))
+        _lib.call("vmc_zgemv", 1, _lib.ptr(U), U.stride(1), P, _lib.ptr(f), _lib.ptr(vtf), _lib.ptr(ws), ws.numel(),
+                  _lib.stream())
+        return vtf
+
+    def _eigh_fp32(self, A):
+        """Stage 1: complex64 eigendecomposition of A, widened (vmc_eigh_fp32)."""
+        P = A.shape[0]
+        dev = A.device
+        ev = torch.empty(P, dtype=torch.float64, device=dev)
+        U = torch.empty((P, P), dtype=torch.complex128, device=dev).mT  # column-major
+        info = torch.zeros(1, dtype=torch.int32, device=dev)
+        ws = _lib.Workspace.get(_lib.query("vmc_eigh_fp32_workspace_bytes", P))
+        _lib.call("vmc_eigh_fp32", P, _lib.ptr(A), A.stride(0), _lib.ptr(ev), _lib.ptr(U), U.stride(1),
+                  _lib.ptr(ws), ws.numel(), _lib.ptr(info), _lib.stream())
+        if int(info.item()) != 0:
+            raise _lib.VmcError("TDVP: the FP32 eigensolver did not converge (info %d)" % int(info.item()))
+        return ev, U
+
+    def _eigh_refine(self, A, ev, U, k, steps, status):
+        """Stage 2: the top k eigenpairs FP64-accurate (vmc_eigh_refine_top)."""
+        P = A.shape[0]
+        info = torch.zeros(1, dtype=torch.int32, device=A.device)
+        ws = _lib.Workspace.get(_lib.query("vmc_eigh_refine_workspace_bytes", P, k))
+        _lib.call("vmc_eigh_refine_top", P, _lib.ptr(A), A.stride(0), k, steps, _lib.ptr(ev), _lib.ptr(U),
+                  U.stride(1), _lib.ptr(ws), ws.numel(), _lib.ptr(status), _lib.ptr(info), _lib.stream())
+        if int(info.item()) != 0:
+            raise _lib.VmcError("TDVP: the FP64 Rayleigh-Ritz eigensolver failed (info %d)" % int(info.item()))
 
     def _status_word(self, dev):
         """Device int32 that a tensor-core kernel of this solver sets when one
