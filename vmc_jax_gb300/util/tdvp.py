@@ -268,7 +268,7 @@ class TDVP:
                                self.snrTol)
             weight = None
             if plan is not None:
-                TIMER.mark("eigh")
+                TIMER.mark("eigh_refine")
                 self._eigh_refine(A, ev, U, plan[0], plan[1], status)
                 vtf = self._project(U, f)
                 TIMER.mark("snr")
