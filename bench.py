@@ -161,7 +161,8 @@ def one_step(ctx, theta):
 
 
 def accuracy_block(ctx):
-    """Relative errors of the mixed and plain-FP32 forms against the FP64
+    """Relative errors of the mixed form (BF16x3 S/SNR; and, as a study, plain
+    BF16 S/SNR: "mixed_bf16x1") and of the plain-FP32 form against the FP64
     form on one common sample: energy and variance of E_loc, S (the complex
     P x P matrix A, Frobenius norm), F (covar(O, E)), and the update dtheta
     (l2 norm and largest entry).  Every form runs its own E_loc kernels
@@ -176,8 +177,11 @@ def accuracy_block(ctx):
     def rel(a, b):
         return float(torch.linalg.norm((a - b).reshape(-1)) / torch.linalg.norm(b.reshape(-1)))
 
-    for prec in ("fp64", "mixed", "fp32"):
+    for form in ("fp64", "mixed", "mixed_bf16x1", "fp32"):
+        prec = "mixed" if form.startswith("mixed") else form
         td = V.util.TDVP(smp, makeReal="real", rhsPrefactor=1., pinvCutoff=1e-8, snrTol=2, precision=prec)
+        if form == "mixed_bf16x1":
+            td.splitProducts = 1
         psi.precision = "fp64" if prec == "fp64" else "fp32"
         psi._touch()
         E = V.operator.BranchFreeOperator.get_O_loc_fused(H, configs, psi, None, 0.)
@@ -187,14 +191,14 @@ def accuracy_block(ctx):
         if ref is None:
             ref = cur
             continue
-        errs[prec] = {"energy": abs(cur["E"] - ref["E"]) / abs(ref["E"]),
+        errs[form] = {"energy": abs(cur["E"] - ref["E"]) / abs(ref["E"]),
                       "variance": abs(cur["var"] - ref["var"]) / abs(ref["var"]),
                       "S": rel(cur["A"], ref["A"]), "F": rel(cur["f"], ref["f"]),
                       "dtheta": rel(cur["u"], ref["u"]),
                       "dtheta_max": float((cur["u"] - ref["u"]).abs().max() / ref["u"].abs().max()),
                       "pinv_cutoff": cur["cutoff"]}
         if prec == "mixed":
-            errs[prec]["eigensolver"] = td.refineInfo
+            errs[form]["eigensolver"] = td.refineInfo
         del cur
         torch.cuda.empty_cache()
     psi.precision = keep
@@ -492,7 +496,7 @@ def kernel_bench(args):
             lo = (x - hi.float()).to(torch.bfloat16)
             del x
             G = torch.empty((rows, rows), dtype=torch.float32, device=dev)
-            fn = lambda: L_.call("vmc_gram_bf16x3", L_.ptr(hi), L_.ptr(lo), rows, K, K, L_.ptr(G), rows, None, st)
+            fn = lambda: L_.call("vmc_gram_bf16x3", L_.ptr(hi), L_.ptr(lo), rows, K, K, L_.ptr(G), rows, 3, None, st)
             alg = float(rows) * (rows + 1) * K
             hw = 3.0 * rows * rows * K
             shape = {"rows": rows, "k": K}
@@ -506,7 +510,7 @@ def kernel_bench(args):
             cs = torch.empty(n, dtype=torch.float32, device=dev)
             ws = torch.empty(L_.query("vmc_gemm_bf16x3_colsq_workspace_bytes", m, n), dtype=torch.uint8, device=dev)
             fn = lambda: L_.call("vmc_gemm_bf16x3_colsq", L_.ptr(ah), L_.ptr(al), m, K, L_.ptr(bh), L_.ptr(bl), n, K,
-                                 K, L_.ptr(cs), L_.ptr(ws), ws.numel(), None, st)
+                                 K, L_.ptr(cs), L_.ptr(ws), ws.numel(), 3, None, st)
             alg = 2.0 * m * n * K
             hw = 3.0 * alg
             shape = {"m": m, "n": n, "k": K}

@@ -325,6 +325,8 @@ int vmc_tdvp_regularize(const double* ev, const double* vtf, const double* snr, 
  * accumulation in TMEM): x ~ hi + lo, products hi.hi + hi.lo + lo.hi.
  * Operand planes are bf16, row-major with leading dimension ld (elements,
  * a multiple of 8, rows 16-byte aligned); the reduction index is contiguous.
+ * products = 3 forms hi.hi + hi.lo + lo.hi; products = 1 forms hi.hi only
+ * and does not read the lo planes (plain BF16, for accuracy studies).
  * Every wait inside these kernels is bounded (vmc_tc_set_wait_limit); a
  * wait that runs out writes a non-zero code to *status (a device int32 the
  * caller zeroes beforehand; NULL selects the library-wide flag read by
@@ -336,7 +338,7 @@ int vmc_tdvp_regularize(const double* ev, const double* vtf, const double* snr, 
  * a multiple of 4); only 128x256 tiles touching the upper triangle
  * (row <= col) are written; gram must be 16-byte aligned. */
 int vmc_gram_bf16x3(const void* hi, const void* lo, int32_t rows, int32_t k, int64_t ld, float* gram,
-                    int64_t ld_gram, int32_t* status, vmc_stream_t stream);
+                    int64_t ld_gram, int32_t products, int32_t* status, vmc_stream_t stream);
 
 /* SNR transform (stats.py:75-83 via tdvp.py:175-179): colsq[c] =
  * sum_r (sum_j A[r][j] B[c][j])^2 for A (m x k) and B (n x k) given as hi/lo
@@ -347,7 +349,7 @@ int vmc_gram_bf16x3(const void* hi, const void* lo, int32_t rows, int32_t k, int
 size_t vmc_gemm_bf16x3_colsq_workspace_bytes(int32_t m, int32_t n);
 int vmc_gemm_bf16x3_colsq(const void* a_hi, const void* a_lo, int32_t m, int64_t lda, const void* b_hi,
                           const void* b_lo, int32_t n, int64_t ldb, int32_t k, float* colsq, void* workspace,
-                          size_t workspace_bytes, int32_t* status, vmc_stream_t stream);
+                          size_t workspace_bytes, int32_t products, int32_t* status, vmc_stream_t stream);
 
 /* Library-wide error flag of the tensor-core kernels (a bounded wait that
  * ran out in a call given no status word); synchronises the device.

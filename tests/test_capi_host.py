@@ -64,9 +64,9 @@ def test_gram_output_alignment_is_checked_on_the_host():
     error, not a launch."""
     lib = L.load()
     p = ctypes.c_void_p(4096)
-    rc = lib.vmc_gram_bf16x3(p, p, 130, 64, 64, ctypes.c_void_p(4096), 130, None, None)
+    rc = lib.vmc_gram_bf16x3(p, p, 130, 64, 64, ctypes.c_void_p(4096), 130, 3, None, None)
     assert rc == 1 and b"multiple of 4" in lib.vmc_last_error_string()
-    rc = lib.vmc_gram_bf16x3(p, p, 128, 64, 64, ctypes.c_void_p(4100), 128, None, None)
+    rc = lib.vmc_gram_bf16x3(p, p, 128, 64, 64, ctypes.c_void_p(4100), 128, 3, None, None)
     assert rc == 1 and b"16 bytes" in lib.vmc_last_error_string()
 
 

@@ -75,7 +75,7 @@ def test_gram_and_hermitian_at_full_rows(cuda):
     hi, lo = _planes(x, k)
     ldg = (R + 15) // 16 * 16
     G = torch.empty((R, ldg), dtype=torch.float32, device=cuda)
-    Lb.call("vmc_gram_bf16x3", Lb.ptr(hi), Lb.ptr(lo), R, k, k, Lb.ptr(G), ldg, None, Lb.stream())
+    Lb.call("vmc_gram_bf16x3", Lb.ptr(hi), Lb.ptr(lo), R, k, k, Lb.ptr(G), ldg, 3, None, Lb.stream())
     torch.cuda.synchronize()
     assert Lb.query("vmc_tc_error_flag", 1) == 0
     rng = np.random.default_rng(8)
@@ -116,7 +116,7 @@ def test_snr_contraction_at_full_shape(cuda):
     colsq = torch.empty(R, dtype=torch.float32, device=cuda)
     ws = torch.empty(Lb.query("vmc_gemm_bf16x3_colsq_workspace_bytes", N, R), dtype=torch.uint8, device=cuda)
     Lb.call("vmc_gemm_bf16x3_colsq", Lb.ptr(ah), Lb.ptr(al), N, R, Lb.ptr(bh), Lb.ptr(bl), R, R, R, Lb.ptr(colsq),
-            Lb.ptr(ws), ws.numel(), None, Lb.stream())
+            Lb.ptr(ws), ws.numel(), 3, None, Lb.stream())
     torch.cuda.synchronize()
     assert Lb.query("vmc_tc_error_flag", 1) == 0
     v = ah.double() + al.double()

@@ -36,7 +36,7 @@ def test_gram_bf16x3(cuda, rows, k):
     hi, lo = _planes(x, ld)
     ldg = (rows + 15) // 16 * 16
     G = torch.full((rows, ldg), float("nan"), dtype=torch.float32, device=cuda)
-    L.call("vmc_gram_bf16x3", L.ptr(hi), L.ptr(lo), rows, k, ld, L.ptr(G), ldg, None, L.stream())
+    L.call("vmc_gram_bf16x3", L.ptr(hi), L.ptr(lo), rows, k, ld, L.ptr(G), ldg, 3, None, L.stream())
     torch.cuda.synchronize()
     assert L.query("vmc_tc_error_flag", 1) == 0
     ref = _split_product(hi, lo, hi, lo, k)
@@ -63,10 +63,10 @@ def test_gemm_bf16x3_colsq(cuda, m, n, k):
     colsq = torch.full((n,), float("nan"), dtype=torch.float32, device=cuda)
     ws = torch.empty(L.query("vmc_gemm_bf16x3_colsq_workspace_bytes", m, n), dtype=torch.uint8, device=cuda)
     L.call("vmc_gemm_bf16x3_colsq", L.ptr(ah), L.ptr(al), m, ld, L.ptr(bh), L.ptr(bl), n, ld, k, L.ptr(colsq),
-           L.ptr(ws), ws.numel(), None, L.stream())
+           L.ptr(ws), ws.numel(), 3, None, L.stream())
     first = colsq.clone()
     L.call("vmc_gemm_bf16x3_colsq", L.ptr(ah), L.ptr(al), m, ld, L.ptr(bh), L.ptr(bl), n, ld, k, L.ptr(colsq),
-           L.ptr(ws), ws.numel(), None, L.stream())
+           L.ptr(ws), ws.numel(), 3, None, L.stream())
     torch.cuda.synchronize()
     assert torch.equal(first, colsq)  # fixed-order reduction: bitwise reproducible
     assert L.query("vmc_tc_error_flag", 1) == 0
@@ -123,9 +123,30 @@ def test_bounded_wait_runs_out_and_reports(cuda):
     hi, lo = _planes(x, 128)
     G = torch.full((256, 256), float("nan"), dtype=torch.float32, device=cuda)
     ok = torch.zeros(1, dtype=torch.int32, device=cuda)
-    L.call("vmc_gram_bf16x3", L.ptr(hi), L.ptr(lo), 256, 128, 128, L.ptr(G), 256, L.ptr(ok), L.stream())
+    L.call("vmc_gram_bf16x3", L.ptr(hi), L.ptr(lo), 256, 128, 128, L.ptr(G), 256, 3, L.ptr(ok), L.stream())
     torch.cuda.synchronize()
     assert int(ok.item()) == 0
     ref = _split_product(hi, lo, hi, lo, 128)
     iu = torch.triu_indices(256, 256, device=cuda)
     assert torch.allclose(G.double()[iu[0], iu[1]], ref[iu[0], iu[1]], rtol=0, atol=2e-5 * ref.abs().max().item())
+
+
+def test_gram_plain_bf16(cuda):
+    """products = 1: the hi planes alone (plain BF16), lo planes not read
+    (here filled with NaN to show it)."""
+    import vmc_jax_gb300._lib as L
+    torch.manual_seed(4)
+    rows, k = 600, 1000
+    ld = (k + 63) // 64 * 64
+    x = torch.randn(rows, k, device=cuda)
+    hi, lo = _planes(x, ld)
+    lo.fill_(float("nan"))
+    ldg = (rows + 15) // 16 * 16
+    G = torch.full((rows, ldg), float("nan"), dtype=torch.float32, device=cuda)
+    L.call("vmc_gram_bf16x3", L.ptr(hi), L.ptr(lo), rows, k, ld, L.ptr(G), ldg, 1, None, L.stream())
+    torch.cuda.synchronize()
+    ref = hi[:, :k].double() @ hi[:, :k].double().T
+    iu = torch.triu_indices(rows, rows, device=cuda)
+    got = G[:, :rows].double()[iu[0], iu[1]]
+    assert torch.isfinite(got).all()
+    assert ((got - ref[iu[0], iu[1]]).abs().max() / ref.abs().max()).item() < 2e-5

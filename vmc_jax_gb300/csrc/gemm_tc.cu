@@ -12,7 +12,8 @@
 //
 // Every operand x is given as two BF16 planes x ~ hi + lo and the product is
 // formed as hi.hi + hi.lo + lo.hi accumulating into the same FP32 TMEM tile:
-// about 16 significant bits per operand instead of 8.
+// about 16 significant bits per operand instead of 8 (products = 3), or as
+// hi.hi alone with the lo planes not read (products = 1: plain BF16).
 //
 // Tile: 128 x 256 x 64 (one tcgen05.mma M=128 N=256 per 16-wide K slice).
 // A pipeline stage holds all four operand tiles of one 64-wide K block
@@ -158,6 +159,7 @@ struct tc_args {
   float* out;         // mode 0: D (row-major, ld = ldOut); mode 1: partial column sums (tilesM * 4, N)
   int64_t ldOut;
   int* status;        // receives the code of a wait that ran out (NULL: the library-wide flag)
+  int products;       // 3: hi.hi + hi.lo + lo.hi; 1: hi.hi only (lo planes not read)
 };
 
 __global__ void __launch_bounds__(TC_THREADS, 1)
@@ -208,13 +210,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         ok = mbar_wait(smem_u32(&bars[TC_STAGES + s]), ph ^ 1u, 1, a.status);
         if (!ok) break;
         const uint32_t full = smem_u32(&bars[s]);
-        mbar_expect_tx(full, TC_STAGE_BYTES);
+        mbar_expect_tx(full, a.products == 1 ? TC_A_BYTES + TC_B_BYTES : TC_STAGE_BYTES);
         const int kb = it;
         unsigned char* st = smem + s * TC_STAGE_BYTES;
         tma_load_2d(smem_u32(st), &mapAhi, kb * TC_BK, tm * TC_BM, full);
-        tma_load_2d(smem_u32(st + TC_A_BYTES), &mapAlo, kb * TC_BK, tm * TC_BM, full);
         tma_load_2d(smem_u32(st + 2 * TC_A_BYTES), &mapBhi, kb * TC_BK, tn * TC_BN, full);
-        tma_load_2d(smem_u32(st + 2 * TC_A_BYTES + TC_B_BYTES), &mapBlo, kb * TC_BK, tn * TC_BN, full);
+        if (a.products != 1) {
+          tma_load_2d(smem_u32(st + TC_A_BYTES), &mapAlo, kb * TC_BK, tm * TC_BM, full);
+          tma_load_2d(smem_u32(st + 2 * TC_A_BYTES + TC_B_BYTES), &mapBlo, kb * TC_BK, tn * TC_BN, full);
+        }
         ++issued;
       }
       if (!ok) {
@@ -242,8 +246,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           // advance the start address by k * 16 bf16 = 32 bytes inside the swizzle atom
           const uint64_t o = (uint64_t)(2 * k);
           mma_bf16(tmem, dah + o, dbh + o, idesc, (it > 0 || k > 0) ? 1u : 0u);
-          mma_bf16(tmem, dah + o, dbl + o, idesc, 1u);
-          mma_bf16(tmem, dal + o, dbh + o, idesc, 1u);
+          if (a.products != 1) {
+            mma_bf16(tmem, dah + o, dbl + o, idesc, 1u);
+            mma_bf16(tmem, dal + o, dbh + o, idesc, 1u);
+          }
         }
         mma_commit(smem_u32(&bars[TC_STAGES + s]));
       }
@@ -369,7 +375,9 @@ static int launch_tc(const CUtensorMap& ah, const CUtensorMap& al, const CUtenso
 using namespace vmc;
 
 extern "C" int vmc_gram_bf16x3(const void* hi, const void* lo, int32_t rows, int32_t k, int64_t ld, float* gram,
-                               int64_t ld_gram, int32_t* status, vmc_stream_t stream) {
+                               int64_t ld_gram, int32_t products, int32_t* status, vmc_stream_t stream) {
+  VMC_REQUIRE(products == 1 || products == 3, VMC_ERR_INVALID_ARGUMENT,
+              "vmc_gram_bf16x3: products must be 1 or 3, not %d", products);
   VMC_REQUIRE(hi && lo && gram && rows > 0 && k > 0 && ld_gram >= rows, VMC_ERR_INVALID_ARGUMENT,
               "vmc_gram_bf16x3: bad arguments");
   VMC_REQUIRE(ld_gram % 4 == 0 && ((uintptr_t)gram & 15) == 0, VMC_ERR_INVALID_ARGUMENT,
@@ -391,6 +399,7 @@ extern "C" int vmc_gram_bf16x3(const void* hi, const void* lo, int32_t rows, int
   a.out = gram;
   a.ldOut = ld_gram;
   a.status = status;
+  a.products = products;
   return launch_tc(mh, ml, nh, nl, a, (int)tile_count(0, a.tilesM, a.tilesN), as_stream(stream));
 }
 
@@ -411,8 +420,10 @@ extern "C" size_t vmc_gemm_bf16x3_colsq_workspace_bytes(int32_t m, int32_t n) {
 
 extern "C" int vmc_gemm_bf16x3_colsq(const void* a_hi, const void* a_lo, int32_t m, int64_t lda, const void* b_hi,
                                      const void* b_lo, int32_t n, int64_t ldb, int32_t k, float* colsq,
-                                     void* workspace, size_t workspace_bytes, int32_t* status,
+                                     void* workspace, size_t workspace_bytes, int32_t products, int32_t* status,
                                      vmc_stream_t stream) {
+  VMC_REQUIRE(products == 1 || products == 3, VMC_ERR_INVALID_ARGUMENT,
+              "vmc_gemm_bf16x3_colsq: products must be 1 or 3, not %d", products);
   VMC_REQUIRE(a_hi && a_lo && b_hi && b_lo && colsq && m > 0 && n > 0 && k > 0, VMC_ERR_INVALID_ARGUMENT,
               "vmc_gemm_bf16x3_colsq: bad arguments");
   VMC_REQUIRE(workspace && workspace_bytes >= vmc_gemm_bf16x3_colsq_workspace_bytes(m, n), VMC_ERR_WORKSPACE,
@@ -433,6 +444,7 @@ extern "C" int vmc_gemm_bf16x3_colsq(const void* a_hi, const void* a_lo, int32_t
   a.out = reinterpret_cast<float*>(workspace);
   a.ldOut = 0;
   a.status = status;
+  a.products = products;
   int rc2 = launch_tc(ah, al, bh, bl, a, (int)tile_count(1, a.tilesM, a.tilesN), as_stream(stream));
   if (rc2) return rc2;
   colsq_reduce_kernel<<<(n + 255) / 256, 256, 0, as_stream(stream)>>>(reinterpret_cast<const float*>(workspace),

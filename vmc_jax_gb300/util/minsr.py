@@ -59,7 +59,7 @@ def tangent_kernel_mixed(X):
     G = torch.empty((R, ldg), dtype=torch.float32, device=dev)
     status = torch.zeros(1, dtype=torch.int32, device=dev)
     st = _lib.stream()
-    _lib.call("vmc_gram_bf16x3", _lib.ptr(hi), _lib.ptr(lo), R, P, ld, _lib.ptr(G), ldg, _lib.ptr(status), st)
+    _lib.call("vmc_gram_bf16x3", _lib.ptr(hi), _lib.ptr(lo), R, P, ld, _lib.ptr(G), ldg, 3, _lib.ptr(status), st)
     del hi, lo
     A = torch.empty((N, N), dtype=torch.complex128, device=dev)
     _lib.call("vmc_gram_to_hermitian", _lib.VMC_F32, _lib.ptr(G), ldg, N, 0.0, _lib.ptr(A), st)

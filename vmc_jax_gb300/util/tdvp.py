@@ -172,6 +172,9 @@ class TDVP:
         self.makeRealName = makeReal
         self.makeReal = imagFun if makeReal == 'imag' else realFun
         self.timings = {}
+        # BF16 products of the mixed S build and SNR contraction: 3 (hi/lo
+        # split correction) or 1 (plain BF16; accuracy studies)
+        self.splitProducts = 3
 
     def set_diagonal_shift(self, delta):
         self.diagonalShift = delta
@@ -441,7 +444,7 @@ class TDVP:
     def _gram(self, data, w, okMean, shift, status=None):
         if self.precision == "mixed":
             from . import gram as _gram
-            return _gram.mixed_hermitian(data, w, okMean, shift, status)
+            return _gram.mixed_hermitian(data, w, okMean, shift, status, self.splitProducts)
         fmt, dt = (0, torch.complex128) if self.precision == "fp64" else (1, torch.complex64)
         X = torch.empty((data.N, data.P), dtype=dt, device=data.device)
         data.centered(w, okMean, fmt, X, None, data.P)
@@ -459,7 +462,7 @@ class TDVP:
         snr = torch.empty(P, dtype=torch.float64, device=dev)
         if self.precision == "mixed":
             from . import gram as _gram
-            colsq = _gram.mixed_snr_colsq(data, w, okMean, E, emean, f, U, x, status)
+            colsq = _gram.mixed_snr_colsq(data, w, okMean, E, emean, f, U, x, status, self.splitProducts)
             realRep, cprec = 1, _lib.VMC_F32
         else:
             fmt, dt = (0, torch.complex128) if self.precision == "fp64" else (1, torch.complex64)
