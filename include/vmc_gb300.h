@@ -368,9 +368,10 @@ int vmc_tc_set_wait_limit(uint64_t limit_ns);
 int vmc_tc_wait_check(uint64_t limit_ns, int32_t* status, vmc_stream_t stream);
 
 /* FP64-accurate complex product on the BF16 tensor cores (Ozaki split):
- * C = op(A) B (+ C when accumulate != 0), A, B, C complex128 column-major;
- * trans_a 'C' (67): op(A) = A^H with A k x m; 'N' (78): op(A) = A with A
- * m x k.  Every operand column is scaled by a power of two and cut into
+ * C = op(A) op(B) (+ C when accumulate != 0), A, B, C complex128
+ * column-major; trans_a 'C' (67): op(A) = A^H with A k x m; 'N' (78):
+ * op(A) = A with A m x k; trans_b 'N': op(B) = B with B k x n; 'C':
+ * op(B) = B^H with B n x k.  Every operand column is scaled by a power of two and cut into
  * `slices` (1..8) slices of 7 bits; slice pairs up to level max_level
  * (<= 2 (slices - 1)) are summed exactly (FP32 tensor-core groups that stay
  * below 2^24 units, int64 sums).  slices 8, max_level 7 give entries
@@ -381,10 +382,10 @@ int vmc_tc_wait_check(uint64_t limit_ns, int32_t* status, vmc_stream_t stream);
  * other tensor-core kernels.  Replaces the O(n^3) products of the
  * eigendecomposition behind tdvp.py:157 (jnp.linalg.eigh). */
 size_t vmc_zgemm_ozaki_workspace_bytes(int32_t m, int32_t n, int32_t k, int32_t slices);
-int vmc_zgemm_ozaki(int32_t trans_a, int32_t m, int32_t n, int32_t k, const double* A, int64_t lda, const double* B,
-                    int64_t ldb, double* C, int64_t ldc, int32_t hermitian, int32_t accumulate, int32_t slices,
-                    int32_t max_level, void* workspace, size_t workspace_bytes, int32_t* status,
-                    vmc_stream_t stream);
+int vmc_zgemm_ozaki(int32_t trans_a, int32_t trans_b, int32_t m, int32_t n, int32_t k, const double* A,
+                    int64_t lda, const double* B, int64_t ldb, double* C, int64_t ldc, int32_t hermitian,
+                    int32_t accumulate, int32_t slices, int32_t max_level, void* workspace, size_t workspace_bytes,
+                    int32_t* status, vmc_stream_t stream);
 
 /* Eigendecomposition of the Hermitian S of the TDVP solve (tdvp.py:153-171,
  * jnp.linalg.eigh), first stage: the complex64 eigendecomposition of A

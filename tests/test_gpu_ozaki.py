@@ -15,7 +15,7 @@ import torch
 pytestmark = pytest.mark.gpu
 
 
-def _ozaki(L, trans, A, B, m, n, k, herm=False, slices=8, level=7, C=None, acc=False):
+def _ozaki(L, trans, A, B, m, n, k, herm=False, slices=8, level=7, C=None, acc=False, trans_b="N"):
     dev = A.device
     nb = L.query("vmc_zgemm_ozaki_workspace_bytes", m, n, k, slices)
     ws = torch.empty(nb + 256, dtype=torch.uint8, device=dev)
@@ -23,7 +23,7 @@ def _ozaki(L, trans, A, B, m, n, k, herm=False, slices=8, level=7, C=None, acc=F
     if C is None:
         C = torch.full((n, m), complex(float("nan"), 0.0), dtype=torch.complex128, device=dev)  # column-major m x n
     status = torch.zeros(1, dtype=torch.int32, device=dev)
-    L.call("vmc_zgemm_ozaki", ord(trans), m, n, k, L.ptr(A), A.shape[1], L.ptr(B), B.shape[1], L.ptr(C), m,
+    L.call("vmc_zgemm_ozaki", ord(trans), ord(trans_b), m, n, k, L.ptr(A), A.shape[1], L.ptr(B), B.shape[1], L.ptr(C), m,
            1 if herm else 0, 1 if acc else 0, slices, level, ws.data_ptr() + base, nb, L.ptr(status), L.stream())
     torch.cuda.synchronize()
     assert int(status.item()) == 0
@@ -50,6 +50,20 @@ def test_product_matches_fp64(cuda, m, n, k, trans):
     scale = opA.abs().square().sum(1).sqrt()[:, None] * Bm.abs().square().sum(0).sqrt()[None, :]
     err = ((got - want).abs() / scale).max().item()
     assert err < 2.0 ** -48, err
+
+
+def test_adjoint_b_operand(cuda):
+    """trans_b 'C': op(B) = B^H with B stored n x k (the layout of a
+    row-major samples x parameters matrix read as its transpose)."""
+    import vmc_jax_gb300._lib as L
+    g = torch.Generator(device=cuda).manual_seed(11)
+    m, n, k = 300, 260, 900
+    Mt = torch.randn(m, k, dtype=torch.complex128, device=cuda, generator=g)
+    Bs = torch.randn(n, k, dtype=torch.complex128, device=cuda, generator=g)   # stored B (n x k)
+    got = _ozaki(L, "N", _colmajor(Mt), _colmajor(Bs), m, n, k, trans_b="C")
+    want = Mt @ Bs.conj().T
+    scale = Mt.abs().square().sum(1).sqrt()[:, None] * Bs.abs().square().sum(1).sqrt()[None, :]
+    assert ((got - want).abs() / scale).max().item() < 2.0 ** -48
 
 
 def test_hermitian_and_accumulate(cuda):

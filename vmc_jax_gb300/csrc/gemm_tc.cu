@@ -751,14 +751,15 @@ extern "C" size_t vmc_zgemm_ozaki_workspace_bytes(int32_t m, int32_t n, int32_t 
   return zgemm_ozaki_ws(m, n, k, slices);
 }
 
-extern "C" int vmc_zgemm_ozaki(int32_t trans_a, int32_t m, int32_t n, int32_t k, const double* A, int64_t lda,
-                               const double* B, int64_t ldb, double* C, int64_t ldc, int32_t hermitian,
+extern "C" int vmc_zgemm_ozaki(int32_t trans_a, int32_t trans_b, int32_t m, int32_t n, int32_t k, const double* A,
+                               int64_t lda, const double* B, int64_t ldb, double* C, int64_t ldc, int32_t hermitian,
                                int32_t accumulate, int32_t slices, int32_t max_level, void* workspace,
                                size_t workspace_bytes, int32_t* status, vmc_stream_t stream) {
-  VMC_REQUIRE(trans_a == 'N' || trans_a == 'C', VMC_ERR_INVALID_ARGUMENT,
-              "vmc_zgemm_ozaki: trans_a must be 'N' or 'C'");
+  VMC_REQUIRE((trans_a == 'N' || trans_a == 'C') && (trans_b == 'N' || trans_b == 'C'), VMC_ERR_INVALID_ARGUMENT,
+              "vmc_zgemm_ozaki: trans_a and trans_b must be 'N' or 'C'");
   VMC_REQUIRE(A && B && C && m > 0 && n > 0 && k > 0, VMC_ERR_INVALID_ARGUMENT, "vmc_zgemm_ozaki: bad arguments");
-  VMC_REQUIRE(lda >= (trans_a == 'N' ? m : k) && ldb >= k && ldc >= m, VMC_ERR_INVALID_ARGUMENT,
+  VMC_REQUIRE(lda >= (trans_a == 'N' ? m : k) && ldb >= (trans_b == 'N' ? k : n) && ldc >= m,
+              VMC_ERR_INVALID_ARGUMENT,
               "vmc_zgemm_ozaki: leading dimension too small");
   VMC_REQUIRE(!hermitian || m == n, VMC_ERR_INVALID_ARGUMENT, "vmc_zgemm_ozaki: a Hermitian product is square");
   VMC_REQUIRE(slices >= 1 && slices <= OZ_MAX_SLICES && max_level >= 0 && max_level <= 2 * (slices - 1),
@@ -785,7 +786,12 @@ extern "C" int vmc_zgemm_ozaki(int32_t trans_a, int32_t m, int32_t n, int32_t k,
   else
     rc = oz_slice(A, lda, 1, 1, oa, false, st);
   if (rc) return rc;
-  if ((rc = oz_slice(B, 1, ldb, 0, ob, true, st))) return rc;
+  // Q[kk][nn] = op(B)[kk][nn]: 'N' -> B[kk + nn ldb]; 'C' -> conj(B[nn + kk ldb])
+  if (trans_b == 'N')
+    rc = oz_slice(B, 1, ldb, 0, ob, true, st);
+  else
+    rc = oz_slice(B, ldb, 1, 1, ob, true, st);
+  if (rc) return rc;
   if ((rc = oz_multiply(oa, ob, max_level, hermitian != 0, out, status, st))) return rc;
   return oz_finish(out, oa, ob, hermitian != 0, C, ldc, accumulate != 0, st, 1.0);
 }

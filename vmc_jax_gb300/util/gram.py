@@ -59,3 +59,22 @@ def mixed_snr_colsq(data, w, okMean, E, emean, f, U, x, status=None, products=3)
               _lib.ptr(colsq), _lib.ptr(ws), ws.numel(), products, _lib.ptr(status), st)
     TIMER.mark("snr_tail")
     return colsq
+
+
+OZAKI_MIN_DIM = 1024   # below this the FP64 product goes through cuBLAS
+
+
+def fp64_product(trans_a, A, lda, trans_b, B, ldb, m, n, k, hermitian=False, status=None):
+    """C = op(A) op(B) as the FP64-accurate tensor-core product
+    (vmc_zgemm_ozaki: 8 slices, levels <= 7, entries within ~2^-48 of the
+    row and column scales).  A, B: complex128 device storage read with the
+    given leading dimensions; returns the column-major m x n result as an
+    (n, m) tensor (its .T is C)."""
+    dev = A.device
+    nb = _lib.query("vmc_zgemm_ozaki_workspace_bytes", m, n, k, 8)
+    ws = _lib.Workspace.get(nb + 256)
+    base = ws.data_ptr() + (256 - ws.data_ptr() % 256) % 256
+    C = torch.empty((n, m), dtype=torch.complex128, device=dev)
+    _lib.call("vmc_zgemm_ozaki", ord(trans_a), ord(trans_b), m, n, k, _lib.ptr(A), lda, _lib.ptr(B), ldb,
+              _lib.ptr(C), m, 1 if hermitian else 0, 0, 8, 7, base, nb, _lib.ptr(status), _lib.stream())
+    return C

@@ -445,10 +445,17 @@ class TDVP:
         if self.precision == "mixed":
             from . import gram as _gram
             return _gram.mixed_hermitian(data, w, okMean, shift, status, self.splitProducts)
+        from . import gram as _gram
         fmt, dt = (0, torch.complex128) if self.precision == "fp64" else (1, torch.complex64)
         X = torch.empty((data.N, data.P), dtype=dt, device=data.device)
         data.centered(w, okMean, fmt, X, None, data.P)
-        A = torch.matmul(X.mH, X).to(torch.complex128)
+        N, P = data.N, data.P
+        if self.precision == "fp64" and P >= _gram.OZAKI_MIN_DIM:
+            # X row-major (N x P) is M = X^T column-major; M M^H = conj(A),
+            # whose column-major storage read row-major is A
+            A = _gram.fp64_product("N", X, P, "C", X, P, P, P, N, hermitian=True, status=status)
+        else:
+            A = torch.matmul(X.mH, X).to(torch.complex128)
         del X
         if shift:
             A.diagonal().mul_(1.0 + shift)
@@ -465,10 +472,15 @@ class TDVP:
             colsq = _gram.mixed_snr_colsq(data, w, okMean, E, emean, f, U, x, status, self.splitProducts)
             realRep, cprec = 1, _lib.VMC_F32
         else:
+            from . import gram as _gram
             fmt, dt = (0, torch.complex128) if self.precision == "fp64" else (1, torch.complex64)
             H = torch.empty((data.N, P), dtype=dt, device=dev)
             data.snr_data(w, okMean, E, emean, -x, f, fmt, H, None, P)
-            Y = torch.matmul(H, torch.conj(U).to(dt))
+            if self.precision == "fp64" and P >= _gram.OZAKI_MIN_DIM and U.stride(0) == 1:
+                # Y^T = U^H H^T (P x N column-major) is Y (N x P) row-major
+                Y = _gram.fp64_product("C", U, U.stride(1), "N", H, P, P, data.N, P, status=status)
+            else:
+                Y = torch.matmul(H, torch.conj(U).to(dt))
             del H
             colsq = (Y.real ** 2 + Y.imag ** 2).sum(0).to(torch.float64).contiguous()
             del Y
