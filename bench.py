@@ -65,6 +65,10 @@ def parse():
     ap.add_argument("--jobs", type=int, default=16)
     ap.add_argument("--rate", type=float, default=2.0, help="job arrivals per second (--serve)")
     ap.add_argument("--job-steps", type=int, default=10)
+    ap.add_argument("--serve-L", default="16,24,32,48,64", help="lattice sizes of the served jobs")
+    ap.add_argument("--serve-m-over-l", default="1,2,4", help="hidden units per site of the served jobs")
+    ap.add_argument("--serve-ns-exp", default="11,14", help="log2 of the smallest and largest sample count")
+    ap.add_argument("--slots", type=int, default=8, help="resident jobs at most (serving)")
     ap.add_argument("--quench", type=float, default=None,
                     help="XXZ L=48 real-time quench with the adaptive Heun integrator up to this time: energy drift "
                          "of the mixed form and of the FP64 form")
@@ -693,35 +697,40 @@ def quench_bench(args):
 
 
 def serve_bench(args):
-    """Poisson arrivals of independent jobs (L in {16, 24, 32}, h ~ U[0.5, 1.5],
-    M in {1, 2} L, N_s in {2^11, 2^12, 2^13}, ground-state or quench) served by
-    the continuous-batching loop; p50/p99 per-step and per-job latency."""
+    """Poisson arrivals of independent jobs served by the continuous-batching
+    loop: the serving workload's distributions (L uniform over --serve-L,
+    h ~ U[0.5, 1.5], M = L times a draw from --serve-m-over-l, N_s = 2^e with
+    e uniform in --serve-ns-exp, 1 in 4 a real-time quench), --job-steps
+    TDVP steps each; p50/p99 per-step and per-job latency and steps/s."""
     import torch
     from vmc_jax_gb300.serving import JobSpec, Server
     torch.cuda.set_device(0)
+    Ls = [int(x) for x in args.serve_L.split(",")]
+    mol = [int(x) for x in args.serve_m_over_l.split(",")]
+    e0, e1 = (int(x) for x in args.serve_ns_exp.split(","))
     rng = np.random.default_rng(123)
     t = 0.0
     specs = []
     for j in range(args.jobs):
         t += rng.exponential(1.0 / args.rate)
-        L = int(rng.choice([16, 24, 32]))
-        specs.append(JobSpec(L=L, h=float(rng.uniform(0.5, 1.5)), M=int(rng.choice([1, 2])) * L,
-                             num_samples=int(2 ** rng.integers(11, 14)), steps=args.job_steps, seed=j,
+        L = int(rng.choice(Ls))
+        specs.append(JobSpec(L=L, h=float(rng.uniform(0.5, 1.5)), M=int(rng.choice(mol)) * L,
+                             num_samples=int(2 ** rng.integers(e0, e1 + 1)), steps=args.job_steps, seed=j,
                              kind="quench" if j % 4 == 3 else "ground_state",
                              dt=0.005 if j % 4 == 3 else 0.01, arrival=t, precision=args.precision))
-    # warm-up: one small job compiles nothing but pages in the libraries
+    # warm-up: one small job pages in the libraries
     w = Server(max_slots=1)
     w.submit(JobSpec(L=8, h=1.0, M=8, num_samples=256, steps=2))
     w.run()
-    srv = Server(max_slots=8)
+    srv = Server(max_slots=args.slots)
     for sp in specs:
         srv.submit(sp)
     rep = srv.run()
     emit({"metric": "served TDVP steps/s and p50/p99 latency", "value": rep["steps_per_s"], "unit": "steps/s",
           "n_gpus": 1, "higher_is_better": True, "data": "synthetic (seeded job stream)",
           "config": {"workload": "poisson_ising_jobs", "jobs": args.jobs, "rate_per_s": args.rate,
-                     "steps_per_job": args.job_steps, "L": [16, 24, 32], "M_over_L": [1, 2],
-                     "N_s": [2048, 4096, 8192], "precision": args.precision},
+                     "steps_per_job": args.job_steps, "L": Ls, "M_over_L": mol,
+                     "N_s": [2 ** e0, 2 ** e1], "precision": args.precision, "slots": args.slots},
           **rep})
 
 

@@ -192,6 +192,17 @@ class Workspace:
         key = (device.index, threading.get_ident())
         buf = cls._bufs.get(key)
         if buf is None or buf.numel() < nbytes:
+            cls._bufs.pop(key, None)
+            buf = None
             buf = torch.empty(max(int(nbytes), 1 << 20), dtype=torch.uint8, device=device)
             cls._bufs[key] = buf
         return buf
+
+    @classmethod
+    def release(cls):
+        """Drop the calling thread's buffers (on every device).  A host thread
+        that ends calls this, or its scratch would stay allocated: buffers are
+        kept per thread so that concurrent solvers never share one."""
+        tid = threading.get_ident()
+        for key in [k for k in cls._bufs if k[1] == tid]:
+            cls._bufs.pop(key, None)

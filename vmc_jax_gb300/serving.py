@@ -96,6 +96,8 @@ def footprint_bytes(spec):
     b += 4 * P * P * 16          # A, eigenvectors, eigh workspace (estimate)
     b += 2 * N * P2 * 2          # SNR data planes
     b += 2 * P2 * P2 * 2         # eigenvector planes
+    if P >= 2048:                # two-stage eigensolver: complex64 copy, cuSOLVER and Ozaki-slice workspaces
+        b += 48 * P * P
     b += N * L * 4 * 2 + N * 64  # configs, per-sample scalars
     b += 64 << 20                # statistics workspace, tables, slack
     return b
@@ -420,6 +422,8 @@ class Server:
             slot.solve(ev, t_launch)
         except Exception as e:  # the job fails alone; its slot is released
             err = "%s: %s" % (type(e).__name__, e)
+        finally:
+            _lib.Workspace.release()  # this step's thread ends: its scratch goes with it
         with self.lock:
             if err is not None or slot.id in self.cancelled or slot.finished:
                 slot.job_latency = time.perf_counter() - slot.arrival_wall
