@@ -595,14 +595,17 @@ __global__ void oz_pad_kernel(__nv_bfloat16* planes, int64_t rows, int64_t K2p, 
 }
 
 // C (column-major, ldc) = alpha product (+ C), the product read from the
-// kernel's row-major [Re | Im] output; with hermitian, entries of the column
-// blocks left of the diagonal block come from the mirrored entry, conjugated.
+// kernel's row-major [Re | Im] output; with hermitian, entries below the
+// diagonal come from the mirrored entry, conjugated, and the diagonal is real.
 __global__ void oz_finish_kernel(const double* __restrict__ out, int64_t ldo, int M, int N, int Np, int hermitian,
                                  double2* __restrict__ C, int64_t ldc, int accumulate, double alpha) {
   __shared__ double2 tile[32][33];
   const int i0 = blockIdx.x * 32, j0 = blockIdx.y * 32;
   const int tx = threadIdx.x, ty = threadIdx.y;
-  const bool mirror = hermitian && (j0 / OZ_BN) < (i0 / OZ_BN);
+  // Hermitian output: every entry below the diagonal is the conjugate of its
+  // mirror (computed by the kernel, whose blocks on and above the diagonal
+  // cover it), so the result is exactly Hermitian
+  const bool mirror = hermitian && j0 < i0;
   if (!mirror) {
 #pragma unroll
     for (int r = 0; r < 32; r += 8) {
@@ -626,6 +629,10 @@ __global__ void oz_finish_kernel(const double* __restrict__ out, int64_t ldo, in
     const int j = j0 + ty + r, i = i0 + tx;
     if (i < M && j < N) {
       double2 v = tile[tx][ty + r];
+      if (hermitian && i0 == j0 && j <= i) {  // diagonal tile: lower part from the upper one
+        const double2 u = tile[ty + r][tx];
+        v = j < i ? make_double2(u.x, -u.y) : make_double2(v.x, 0.0);
+      }
       v.x *= alpha;
       v.y *= alpha;
       double2* dst = C + (int64_t)j * ldc + i;

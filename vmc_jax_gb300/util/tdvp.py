@@ -59,10 +59,8 @@ def transform_helper(x, rhsPrefactor, makeReal):
 
 
 REFINE_EXCLUDED_NORM = 1e-12   # weight the FP32-only eigenpairs may carry, relative
-REFINE_CARRY = 1e-6            # components above this fraction of the largest weight carry the solve
 REFINE_MAX_FRACTION = 1.0 / 3  # refine at most this fraction of the spectrum
 REFINE_MAX_RHO = 0.25          # largest |lambda_excluded / lambda_carrying| accepted
-REFINE_GAP_WINDOW = 1.0 / 8    # search window (fraction of n) for the spectral gap below them
 
 
 def solve_weights(ev, vtf, snr, pinvCutoff, snrTol, snrMargin=1.0):
@@ -80,44 +78,43 @@ def solve_weights(ev, vtf, snr, pinvCutoff, snrTol, snrMargin=1.0):
 
 def refine_plan(ev, vtf, snr, pinvCutoff, snrTol):
     """Number k of top eigenpairs to refine to FP64 accuracy and the power
-    steps q, from the FP32 eigendecomposition (ev ascending, vtf = U^H f,
-    snr); None when the FP64 eigensolver of the whole matrix is to be used.
+    steps q, from the FP32 eigendecomposition (ev ascending); None when the
+    FP64 eigensolver of the whole matrix is to be used.
 
-    The components that carry the update (weight >= REFINE_CARRY of the
-    largest, weights from solve_weights) are read off the FP32 values,
-    which are accurate for them.  The split b is the largest relative gap
-    |lambda_b / lambda_(b-1)| of the spectrum at or below the lowest carrying
-    component, within REFINE_GAP_WINDOW n of it.  The FP32 bulk vectors are
-    not used to judge the bulk: their projections carry a ~1e-6 share of the
-    top block (FP32 rotation between the blocks) that inflates their SNR;
-    the bulk's share is checked after the refinement (bulk_weight).  Per
-    power step the FP32 error of a carrying component (~1e-7 lambda_max /
-    gap) shrinks by rho = |lambda_(b-1)| / |lambda_carrying min|."""
+    Only the spectrum is used: FP32 eigenvalues below the FP32 noise floor
+    (the size of the most negative one of this positive semi-definite S,
+    at least 64 u32 lambda_max) are not resolved, and the FP32 bulk vectors
+    carry a ~1e-6 share of the top block that inflates their projections of
+    F and their SNR (which enters to the 6th power), so their weights say
+    nothing about the bulk.  The split b is the largest relative gap
+    |lambda_b / lambda_(b-1)| with lambda_b at least 10x the noise floor and
+    at most REFINE_MAX_FRACTION of the spectrum above it; whether the
+    eigenpairs below it may keep FP32 accuracy is decided after the
+    refinement, from their share of the update (bulk_weight).  Per power step
+    the FP32 error of the refined vectors along the rest (~1e-7 lambda_max /
+    gap) shrinks by rho = lambda_(b-1) / lambda_b.  vtf and snr are not used
+    and kept for the interface."""
     n = ev.shape[0]
-    lmax = np.max(np.abs(ev))
-    if lmax == 0.0:
-        return None
-    c = solve_weights(ev, vtf, snr, pinvCutoff, snrTol)
-    if not np.all(np.isfinite(c)) or c.max() == 0.0:
-        return None
-    j = int(np.nonzero(c >= REFINE_CARRY * c.max())[0].min())
-    if j < 1:
-        return None
-    lo = max(1, j - int(REFINE_GAP_WINDOW * n))
     a = np.abs(ev)
-    cand = np.arange(lo, j + 1)
+    lmax = a.max()
+    if lmax == 0.0 or n < 2:
+        return None
+    noise = max(-float(ev.min()), 0.0) + 64 * 6e-8 * lmax
+    lo = max(1, int(np.ceil((1.0 - REFINE_MAX_FRACTION) * n)))
+    cand = np.arange(lo, n)
+    cand = cand[a[cand] >= 10.0 * noise]
+    if cand.size == 0:
+        return None
     with np.errstate(divide="ignore", invalid="ignore"):
-        ratio = a[cand] / np.maximum(a[cand - 1], 1e-300 * lmax)
+        ratio = a[cand] / np.maximum(a[cand - 1], noise)
     b = int(cand[int(np.argmax(ratio))])
     k = n - b
-    if k > REFINE_MAX_FRACTION * n:
-        return None
-    rho = a[b - 1] / a[j]
+    rho = max(a[b - 1], noise) / a[b]
     if not rho < REFINE_MAX_RHO:
         return None
-    gap = max(a[j] - a[b - 1], 1e-300)
+    gap = max(a[b] - a[b - 1], 1e-300)
     eps0 = min(1.0, 1e-7 * lmax / gap)
-    q = 0 if rho == 0.0 else int(np.ceil(np.log(1e-16 / eps0) / np.log(rho)))
+    q = int(np.ceil(np.log(1e-16 / eps0) / np.log(rho)))
     return k, int(min(max(q, 1), 16))
 
 
@@ -263,7 +260,10 @@ class TDVP:
         self.refineInfo = None
         useSnr = not isinstance(self.sampler, ExactSampler)
         if self._two_stage(realParams, useSnr, P):
-            ev, U = self._eigh_fp32(A)
+            # the C ABI reads matrices column-major: the row-major storage of
+            # conj(A) is A column-major (A Hermitian)
+            Acm = torch.conj_physical(A)
+            ev, U = self._eigh_fp32(Acm)
             vtf = self._project(U, f)
             TIMER.mark("snr")
             snr = self._snr(data, w, okMean, E, emean, f, U, vtf, status)
@@ -272,7 +272,7 @@ class TDVP:
             weight = None
             if plan is not None:
                 TIMER.mark("eigh_refine")
-                self._eigh_refine(A, ev, U, plan[0], plan[1], status)
+                self._eigh_refine(Acm, ev, U, plan[0], plan[1], status)
                 vtf = self._project(U, f)
                 TIMER.mark("snr")
                 snr = self._snr(data, w, okMean, E, emean, f, U, vtf, status)
@@ -280,6 +280,7 @@ class TDVP:
                                      self.pinvCutoff, self.snrTol)
                 if weight > REFINE_EXCLUDED_NORM:
                     plan = None
+            del Acm
             if plan is None:
                 TIMER.mark("eigh")
                 ev, U = torch.linalg.eigh(A)
@@ -351,7 +352,8 @@ class TDVP:
         return vtf
 
     def _eigh_fp32(self, A):
-        """Stage 1: complex64 eigendecomposition of A, widened (vmc_eigh_fp32)."""
+        """Stage 1: complex64 eigendecomposition of A (given column-major),
+        widened (vmc_eigh_fp32)."""
         P = A.shape[0]
         dev = A.device
         ev = torch.empty(P, dtype=torch.float64, device=dev)
@@ -365,7 +367,8 @@ class TDVP:
         return ev, U
 
     def _eigh_refine(self, A, ev, U, k, steps, status):
-        """Stage 2: the top k eigenpairs FP64-accurate (vmc_eigh_refine_top)."""
+        """Stage 2: the top k eigenpairs FP64-accurate (vmc_eigh_refine_top);
+        A given column-major."""
         P = A.shape[0]
         info = torch.zeros(1, dtype=torch.int32, device=A.device)
         ws = _lib.Workspace.get(_lib.query("vmc_eigh_refine_workspace_bytes", P, k))
