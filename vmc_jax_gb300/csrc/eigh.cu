@@ -11,7 +11,8 @@
 //        |lambda_{n-k-1} / lambda_j| per step);
 //        Rayleigh-Ritz in FP64: G = X^H X, H = X^H A X, H c = theta G c
 //        (cuSOLVER zhegvd on k x k);  V_top = X C, ev_top = theta;
-//        V_rest <- V_rest - V_top (V_top^H V_rest), columns renormalised.
+//        V_rest <- V_rest - V_top (V_top^H V_rest), columns renormalised
+//        (orthogonal to V_top to ~1e-12: V_top^H V_rest from 6 slices).
 //      Every O(n^2 k) product runs as an FP64-accurate Ozaki-split product
 //      on the BF16 tensor cores (oz_host.h).  The n - k other eigenvalues
 //      keep their FP32 values (absolute error ~1e-7 of the largest); the
@@ -126,7 +127,8 @@ int grid_for(int64_t total) {
 
 constexpr int kSlices = 8, kLevel = 7;            // FP64-accurate products
 constexpr int kEarlySlices = 6, kEarlyLevel = 5;  // power steps before the last (2^-40 relative)
-constexpr int kRestSlices = 5, kRestLevel = 4;    // corrections of FP32-accurate vectors (2^-33 relative)
+constexpr int kRestSlices = 5, kRestLevel = 4;    // V_top T: T ~ 1e-7, error 2^-33 of |V_top| |T| (negligible)
+constexpr int kProjSlices = 6, kProjLevel = 5;    // T = V_top^H V_rest: error 2^-40 of |V_top| |V_rest| = 1
 constexpr int kRestChunk = 4096;                  // columns of V_rest per orthogonalisation pass
 
 struct refine_layout {
@@ -161,7 +163,7 @@ int refine_layout_for(int n, int k, refine_layout& L, cudaStream_t st) {
   // B-operand buffer: X, Y (k rows, K n) / C (k, K k) / V_rest chunk (rc, K n) / T chunk (rc, K k)
   size_t bBytes = oz_operand_bytes(k, n, kSlices, true);
   if (rc_cols > 0) {
-    const size_t v = oz_operand_bytes(rc_cols, n, kRestSlices, true);
+    const size_t v = oz_operand_bytes(rc_cols, n, kProjSlices, true);
     if (v > bBytes) bBytes = v;
   }
   // second A-operand buffer: X^H (k, K n) for G and H, X (n, K k) for X C, V_top (n, K k)
@@ -343,16 +345,16 @@ extern "C" int vmc_eigh_refine_top(int32_t n, const double* A, int64_t lda, int3
   if (b > 0) {
     oz_operand opVtH, opVtN;
     // V_top^H as A operand (rows k, K n) in bufA (A no longer needed), V_top as A operand (rows n, K k) in bufC
-    oz_make_operand(bufA, k, n, kRestSlices, false, opVtH);
+    oz_make_operand(bufA, k, n, kProjSlices, false, opVtH);
     if ((rc = oz_slice(Vtop, 1, ldv, 0, opVtH, false, st))) return rc;
     oz_make_operand(bufC, n, k, kRestSlices, false, opVtN);
     if ((rc = oz_slice(Vtop, ldv, 1, 1, opVtN, false, st))) return rc;
     for (int c0 = 0; c0 < b; c0 += kRestChunk) {
       const int cols = b - c0 < kRestChunk ? b - c0 : kRestChunk;
       double* Vc = V + 2 * (int64_t)c0 * ldv;
-      oz_make_operand(bufB, cols, n, kRestSlices, true, opB);
+      oz_make_operand(bufB, cols, n, kProjSlices, true, opB);
       if ((rc = oz_slice(Vc, 1, ldv, 0, opB, true, st))) return rc;
-      if ((rc = oz_multiply(opVtH, opB, kRestLevel, false, out, status, st))) return rc;
+      if ((rc = oz_multiply(opVtH, opB, kProjLevel, false, out, status, st))) return rc;
       if ((rc = oz_finish(out, opVtH, opB, false, T, k, false, st, 1.0))) return rc;
       oz_make_operand(bufB, cols, k, kRestSlices, true, opB);
       if ((rc = oz_slice(T, 1, k, 0, opB, true, st))) return rc;
