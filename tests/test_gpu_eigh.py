@@ -107,11 +107,12 @@ def test_refinement_improves_fp32_vectors(cuda):
 def test_tdvp_two_stage_matches_fp64_eigensolver(cuda):
     """The mixed TDVP step with the two-stage eigensolver against the same
     step with cuSOLVER's FP64 eigendecomposition of the same S, on the same
-    Monte Carlo samples (TFIM L=48, h=1, CpxRBM M=64, 4096 samples): the
-    refined block must carry the solve, and the updates agree to 1e-10."""
+    Monte Carlo samples (TFIM L=32, h=1, CpxRBM M=128, 4096 samples; 528 of
+    4224 eigenpairs above the spectral gap): the refined block must carry the
+    solve, and the updates agree to 1e-10."""
     import vmc_jax_gb300 as V
     from vmc_jax_gb300.util import tdvp as T
-    L_, M = 48, 64
+    L_, M = 32, 128
     rng = np.random.default_rng(0)
     b = rng.normal(0, 0.01, M) + 1j * rng.normal(0, 0.01, M)
     W = rng.normal(0, 0.01, (L_, M)) + 1j * rng.normal(0, 0.01, (L_, M))

@@ -17,8 +17,9 @@
 //      on the BF16 tensor cores (oz_host.h).  The n - k other eigenvalues
 //      keep their FP32 values (absolute error ~1e-7 of the largest); the
 //      caller picks k so that the part of the solve they carry is negligible
-//      (util/tdvp.py: spectral gap below the SNR- and cutoff-regularised
-//      weights of step 1, checked again after step 2).
+//      (util/tdvp.py: the largest spectral gap above the FP32 noise floor,
+//      and after step 2 the share of the update left on the unrefined
+//      eigenpairs, which must be below 1e-12).
 //
 // cuSOLVER is called through a handle per device and host thread; its
 // device workspace comes from the caller's workspace, its small host

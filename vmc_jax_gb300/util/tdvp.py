@@ -59,7 +59,7 @@ def transform_helper(x, rhsPrefactor, makeReal):
 
 
 REFINE_EXCLUDED_NORM = 1e-12   # weight the FP32-only eigenpairs may carry, relative
-REFINE_MAX_FRACTION = 1.0 / 3  # refine at most this fraction of the spectrum
+REFINE_MAX_FRACTION = 0.5      # refine at most this fraction of the spectrum
 REFINE_MAX_RHO = 0.25          # largest |lambda_excluded / lambda_carrying| accepted
 
 
