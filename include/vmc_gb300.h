@@ -396,6 +396,15 @@ size_t vmc_eigh_fp32_workspace_bytes(int32_t n);
 int vmc_eigh_fp32(int32_t n, const double* A, int64_t lda, double* ev, double* V, int64_t ldv, void* workspace,
                   size_t workspace_bytes, int32_t* info, vmc_stream_t stream);
 
+/* FP64 eigendecomposition (tdvp.py:157, jnp.linalg.eigh in FP64; the FP64
+ * and plain-FP32 forms, ExactSampler steps, MinSR's pseudo-inverse):
+ * cuSOLVER on A (n x n, column-major, complex128 when is_complex != 0, else
+ * float64), eigenvalues ascending into ev, eigenvectors into V (A is copied
+ * into V first; A may be V).  *info: cuSOLVER's status. */
+size_t vmc_eigh_fp64_workspace_bytes(int32_t n, int32_t is_complex);
+int vmc_eigh_fp64(int32_t n, int32_t is_complex, const double* A, int64_t lda, double* ev, double* V, int64_t ldv,
+                  void* workspace, size_t workspace_bytes, int32_t* info, vmc_stream_t stream);
+
 /* Second stage: on entry ev, V from vmc_eigh_fp32 for the same A.  The k
  * eigenpairs of largest eigenvalue become FP64-accurate: power_steps
  * products X <- A X diag(1/ev) of the top-k vectors, then Rayleigh-Ritz in

@@ -145,3 +145,20 @@ def test_tdvp_two_stage_matches_fp64_eigensolver(cuda):
     assert (ev2[-k:] - td.ev_c[-k:]).abs().max().item() / lmax < 1e-12
     assert float(c1) == float(c2)
     assert rel < 1e-10, rel
+
+
+@pytest.mark.parametrize("cplx", [True, False])
+def test_fp64_eigensolver_matches_torch(cuda, cplx):
+    """vmc_eigh_fp64 (cuSOLVER through the C ABI) against torch.linalg.eigh."""
+    from vmc_jax_gb300.util.gram import eigh_fp64
+    g = torch.Generator(device=cuda).manual_seed(4)
+    n = 300
+    dt = torch.complex128 if cplx else torch.float64
+    Z = torch.randn(n, n, dtype=dt, device=cuda, generator=g)
+    A = (Z @ Z.mH).resolve_conj() if cplx else Z @ Z.T
+    ev, U = eigh_fp64(A)
+    ref, _ = torch.linalg.eigh(A)
+    assert U.stride(0) == 1
+    assert (ev - ref).abs().max().item() / ref.abs().max().item() < 1e-13
+    R = A @ U - U * ev[None, :].to(dt)
+    assert R.abs().max().item() / ref.abs().max().item() < 1e-12

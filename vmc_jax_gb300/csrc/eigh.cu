@@ -367,3 +367,62 @@ extern "C" int vmc_eigh_refine_top(int32_t n, const double* A, int64_t lda, int3
   }
   return VMC_OK;
 }
+
+// ---------------------------------------------------------------------------
+// FP64 eigendecomposition by cuSOLVER (the reference's jnp.linalg.eigh in
+// FP64, tdvp.py:157): complex Hermitian or real symmetric A (column-major);
+// ev ascending, eigenvectors overwrite V (A is copied into V first, so A may
+// alias V).
+// ---------------------------------------------------------------------------
+namespace vmc {
+namespace {
+size_t fp64_device_bytes(int n, int cplx, cudaStream_t st, size_t* hostBytes) {
+  solver_slot* s;
+  if (solver_for(st, &s)) return 0;
+  size_t dev = 0, host = 0;
+  const cudaDataType ta = cplx ? CUDA_C_64F : CUDA_R_64F;
+  if (cusolverDnXsyevd_bufferSize(s->h, s->p, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, ta, nullptr, n,
+                                  CUDA_R_64F, nullptr, ta, &dev, &host) != CUSOLVER_STATUS_SUCCESS)
+    return 0;
+  if (hostBytes) *hostBytes = host;
+  return dev > 0 ? dev : 1;
+}
+}  // namespace
+}  // namespace vmc
+
+extern "C" size_t vmc_eigh_fp64_workspace_bytes(int32_t n, int32_t is_complex) {
+  if (n <= 0) return 0;
+  const size_t dev = fp64_device_bytes(n, is_complex != 0, 0, nullptr);
+  return dev ? align256(dev) + 256 : 0;
+}
+
+extern "C" int vmc_eigh_fp64(int32_t n, int32_t is_complex, const double* A, int64_t lda, double* ev, double* V,
+                             int64_t ldv, void* workspace, size_t workspace_bytes, int32_t* info,
+                             vmc_stream_t stream) {
+  VMC_REQUIRE(n > 0 && A && ev && V && info && lda >= n && ldv >= n, VMC_ERR_INVALID_ARGUMENT,
+              "vmc_eigh_fp64: bad arguments");
+  cudaStream_t st = as_stream(stream);
+  const int cplx = is_complex != 0;
+  size_t hostBytes = 0;
+  const size_t dev = fp64_device_bytes(n, cplx, st, &hostBytes);
+  VMC_REQUIRE(dev > 0, VMC_ERR_CUDA, "vmc_eigh_fp64: cuSOLVER workspace query failed");
+  VMC_REQUIRE(workspace && workspace_bytes >= align256(dev) + 256, VMC_ERR_WORKSPACE,
+              "vmc_eigh_fp64: workspace of %zu bytes needed", align256(dev) + 256);
+  void* dws = reinterpret_cast<void*>((reinterpret_cast<uintptr_t>(workspace) + 255) & ~(uintptr_t)255);
+  const size_t el = cplx ? 16 : 8;
+  if (A != V) {
+    cudaError_t e = cudaMemcpy2DAsync(V, (size_t)ldv * el, A, (size_t)lda * el, (size_t)n * el, n,
+                                      cudaMemcpyDeviceToDevice, st);
+    VMC_REQUIRE(e == cudaSuccess, VMC_ERR_CUDA, "vmc_eigh_fp64: %s", cudaGetErrorString(e));
+  }
+  solver_slot* s;
+  int rc = solver_for(st, &s);
+  if (rc) return rc;
+  std::vector<char>& hb = host_scratch();
+  if (hb.size() < hostBytes + 1) hb.resize(hostBytes + 1);
+  const cudaDataType ta = cplx ? CUDA_C_64F : CUDA_R_64F;
+  const cusolverStatus_t cs = cusolverDnXsyevd(s->h, s->p, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, ta, V,
+                                               ldv, CUDA_R_64F, ev, ta, dws, dev, hb.data(), hostBytes, info);
+  VMC_REQUIRE(cs == CUSOLVER_STATUS_SUCCESS, VMC_ERR_CUDA, "vmc_eigh_fp64: cusolverDnXsyevd failed (%d)", (int)cs);
+  return VMC_OK;
+}

@@ -78,3 +78,23 @@ def fp64_product(trans_a, A, lda, trans_b, B, ldb, m, n, k, hermitian=False, sta
     _lib.call("vmc_zgemm_ozaki", ord(trans_a), ord(trans_b), m, n, k, _lib.ptr(A), lda, _lib.ptr(B), ldb,
               _lib.ptr(C), m, 1 if hermitian else 0, 0, 8, 7, base, nb, _lib.ptr(status), _lib.stream())
     return C
+
+
+def eigh_fp64(A):
+    """FP64 eigendecomposition of the Hermitian (or real symmetric) A (a
+    row-major torch tensor) by cuSOLVER through the C ABI (vmc_eigh_fp64):
+    (ev ascending, U column-major with U[:, j] the eigenvectors), as
+    torch.linalg.eigh(A) returns them."""
+    n = A.shape[0]
+    cplx = A.is_complex()
+    dev = A.device
+    # the C ABI reads column-major: the row-major storage of conj(A) (= A^T) is A
+    V = (torch.conj_physical(A) if cplx else A.T).contiguous()
+    ev = torch.empty(n, dtype=torch.float64, device=dev)
+    info = torch.zeros(1, dtype=torch.int32, device=dev)
+    ws = _lib.Workspace.get(_lib.query("vmc_eigh_fp64_workspace_bytes", n, 1 if cplx else 0))
+    _lib.call("vmc_eigh_fp64", n, 1 if cplx else 0, _lib.ptr(V), n, _lib.ptr(ev), _lib.ptr(V), n, _lib.ptr(ws),
+              ws.numel(), _lib.ptr(info), _lib.stream())
+    if int(info.item()) != 0:
+        raise _lib.VmcError("FP64 eigensolver did not converge (info %d)" % int(info.item()))
+    return ev, V.mT   # V's storage is column-major: the tensor's transpose is the eigenvector matrix

@@ -25,7 +25,8 @@ def pinv_hermitian(T, rtol):
     """jnp.linalg.pinv(T, rtol, hermitian=True) (minsr.py:63,74) by eigh:
     eigenvalues with |l| <= rtol max|l| are dropped.  Returned factored as
     (V, inv): T^+ = V diag(inv) V^dagger."""
-    ev, V = torch.linalg.eigh(T)
+    from .gram import eigh_fp64
+    ev, V = eigh_fp64(T)
     cut = rtol * torch.max(torch.abs(ev))
     inv = torch.where(torch.abs(ev) > cut, 1.0 / ev, torch.zeros_like(ev))
     return V, inv

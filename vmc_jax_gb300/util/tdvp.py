@@ -43,6 +43,11 @@ from ..stats import SampledObs
 from .timing import TIMER
 
 
+def _gram_mod():
+    from . import gram
+    return gram
+
+
 def realFun(x):
     """tdvp.py:14-15."""
     return torch.real(x) if isinstance(x, torch.Tensor) else np.real(x)
@@ -283,7 +288,7 @@ class TDVP:
             del Acm
             if plan is None:
                 TIMER.mark("eigh")
-                ev, U = torch.linalg.eigh(A)
+                ev, U = _gram_mod().eigh_fp64(A)
                 if U.stride(0) != 1:
                     U = U.mT.contiguous().mT
                 vtf = self._project(U, f)
@@ -294,10 +299,10 @@ class TDVP:
                                "fp32_bulk_weight": weight}
         else:
             if realParams:  # S real symmetric: the real eigensolver, vectors as complex
-                ev, U = torch.linalg.eigh(A.real.contiguous())
+                ev, U = _gram_mod().eigh_fp64(A.real.contiguous())
                 U = U.to(torch.complex128)
             else:
-                ev, U = torch.linalg.eigh(A)
+                ev, U = _gram_mod().eigh_fp64(A)
             if U.stride(0) != 1:
                 U = U.mT.contiguous().mT
             vtf = self._project(U, f)
@@ -540,7 +545,7 @@ class TDVP:
         return S, F
 
     def _transform_to_eigenbasis(self, S, F):
-        self.ev, self.V = torch.linalg.eigh(S)
+        self.ev, self.V = _gram_mod().eigh_fp64(S.contiguous())
         self.VtF = torch.matmul(torch.conj(self.V).T, F.to(self.V.dtype))
 
     def _get_snr(self, Eloc, gradients):
