@@ -133,12 +133,42 @@ KERNELS_PER_CALL = {
 launch_count = 0
 
 
+def _slice_launches(K):
+    """Kernels of one Ozaki operand slicing: row exponents, slices, and the
+    padding columns when 2K is not a multiple of 64."""
+    return 2 + (1 if (2 * K) % 64 else 0)
+
+
+def _refine_launches(args):
+    """Kernels of one vmc_eigh_refine_top call (n, A, lda, k, steps, ...)."""
+    n, k, q = int(args[0]), int(args[3]), int(args[4])
+    b = n - k
+    c = _slice_launches(n)                                  # A
+    c += q * (_slice_launches(n) + 3)                       # power steps: slice, product, assembly, scaling
+    c += 3 * (_slice_launches(n) + 2)                       # Y, G, H
+    c += 2 * _slice_launches(k) + 2                         # X C
+    if b > 0:
+        chunks = (b + 4095) // 4096
+        c += _slice_launches(n) + _slice_launches(k)        # V_top^H and V_top
+        c += chunks * (_slice_launches(n) + _slice_launches(k) + 4) + 1
+    return c
+
+
+KERNELS_PER_CALL.update({
+    "vmc_zgemm_ozaki": lambda a: _slice_launches(int(a[4])) * 2 + 2,
+    "vmc_eigh_fp32": 2, "vmc_eigh_fp64": 0, "vmc_eigh_refine_top": _refine_launches,
+    "vmc_tc_wait_check": 1,
+})
+
+
 def call(name, *args):
     """Call a status-returning entry point; raise VmcError on failure."""
     global launch_count
     lib = load()
     rc = getattr(lib, name)(*args)
     n = KERNELS_PER_CALL.get(name, 1)
+    if callable(n):
+        n = n(args)
     if name == "vmc_zgemv" and args and args[0]:
         n = 1  # the adjoint product is one kernel, the plain one two
     launch_count += n
