@@ -108,8 +108,12 @@ def test_tdvp_two_stage_matches_fp64_eigensolver(cuda):
     """The mixed TDVP step with the two-stage eigensolver against the same
     step with cuSOLVER's FP64 eigendecomposition of the same S, on the same
     Monte Carlo samples (TFIM L=32, h=1, CpxRBM M=128, 4096 samples; 528 of
-    4224 eigenpairs above the spectral gap): the refined block must carry the
-    solve, and the updates agree to 1e-10."""
+    4224 eigenpairs above the spectral gap).  The refined block must carry
+    the solve; its eigenvalues agree to 1e-12 of the largest; the updates
+    agree to 1e-10 or 10x the conditioning floor of the solve, measured as
+    the change of the cuSOLVER update when every entry of S moves by one ulp
+    (two eigensolvers may rotate differently inside nearly degenerate pairs,
+    where the per-eigenvector SNR of tdvp.py:173-181 depends on the basis)."""
     import vmc_jax_gb300 as V
     from vmc_jax_gb300.util import tdvp as T
     L_, M = 32, 128
@@ -132,19 +136,31 @@ def test_tdvp_two_stage_matches_fp64_eigensolver(cuda):
     info = td.refineInfo
     ev2 = td.ev_c.clone()
     keep = T.TDVP.TWO_STAGE_MIN_P
+    gram = td._gram
     try:
         T.TDVP.TWO_STAGE_MIN_P = 1 << 30
         u1, r1, c1 = td._complex_rhs(psi, configs, E, p)
+        ev1 = td.ev_c.clone()
+        g = torch.Generator(device=cuda).manual_seed(1)
+
+        def perturbed(*a, **k):
+            A = gram(*a, **k)
+            Ep = torch.randn(A.shape, dtype=torch.float64, device=A.device, generator=g)
+            return A + A * (2.0 ** -52 * 0.5 * (Ep + Ep.T))
+        td._gram = perturbed
+        u0, _, _ = td._complex_rhs(psi, configs, E, p)
     finally:
         T.TDVP.TWO_STAGE_MIN_P = keep
-    print("refinement plan", info)
+        td._gram = gram
+    floor = (torch.linalg.norm(u0 - u1) / torch.linalg.norm(u1)).item()
+    rel = (torch.linalg.norm(u2 - u1) / torch.linalg.norm(u1)).item()
+    print("refinement plan", info, "update difference %.2e, conditioning floor %.2e" % (rel, floor))
     assert info is not None and info["refined"] is not None
     k = info["refined"]
-    rel = (torch.linalg.norm(u2 - u1) / torch.linalg.norm(u1)).item()
-    lmax = td.ev_c.abs().max().item()
-    assert (ev2[-k:] - td.ev_c[-k:]).abs().max().item() / lmax < 1e-12
+    lmax = ev1.abs().max().item()
+    assert (ev2[-k:] - ev1[-k:]).abs().max().item() / lmax < 1e-12
     assert float(c1) == float(c2)
-    assert rel < 1e-10, rel
+    assert rel <= max(1e-10, 10.0 * floor), (rel, floor)
 
 
 @pytest.mark.parametrize("cplx", [True, False])
