@@ -870,9 +870,15 @@ def main():
         fp64eq = flops / full
         t = float(np.mean(refine_ms)) * 1e-3
         peak = peaks.get("bf16_tflops_sustained", 1700.0)
+        # DRAM bytes per executed flop of the ncu capture of one 4096^3
+        # complex product (8 slices, 36 pairs: 1.979e13 flop, 44.02 GB read +
+        # 0.265 GB written), applied to the refinement's executed flop
+        traffic = flops * (44.02e9 + 0.265e9) / (36 * 8.0 * 4096.0 ** 3)
         oz = {"kernel": "oz_gemm_kernel (Ozaki-split FP64-accurate complex products, tcgen05) in "
                         "vmc_eigh_refine_top", "bound": "tensor", "achieved": flops / t / 1e12, "peak": peak,
-              "unit": "TFLOP/s", "frac": flops / t / 1e12 / peak,
+              "unit": "TFLOP/s", "frac": flops / t / 1e12 / peak, "traffic": traffic,
+              "traffic_source": "ncu dram__bytes_read+write per executed flop of the 4096^3 capture, scaled to "
+                                "the refinement's executed flop (all its Ozaki launches)",
               "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained (of measured)",
               "algorithmic_flops_per_refinement": flops, "fp64_equivalent_tflops": fp64eq / t / 1e12,
               "refinement_ms": t * 1e3,

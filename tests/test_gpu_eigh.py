@@ -109,13 +109,20 @@ def test_tdvp_two_stage_matches_fp64_eigensolver(cuda):
     step with cuSOLVER's FP64 eigendecomposition of the same S, on the same
     Monte Carlo samples (TFIM L=32, h=1, CpxRBM M=128, 4096 samples; 528 of
     4224 eigenpairs above the spectral gap).  The refined block must carry
-    the solve; its eigenvalues agree to 1e-12 of the largest; the updates
-    agree to 1e-10 or 10x the conditioning floor of the solve, measured as
-    the change of the cuSOLVER update when every entry of S moves by one ulp
-    (two eigensolvers may rotate differently inside nearly degenerate pairs,
-    where the per-eigenvector SNR of tdvp.py:173-181 depends on the basis)."""
+    the solve and its eigenvalues agree to 1e-12 of the largest.
+
+    Each eigenvector is fixed only up to a phase, and the mixed form's
+    per-eigenvector SNR (tdvp.py:173-181) is a BF16x3 contraction whose
+    rounding depends on that phase: the update moves by ~1e-7 when the
+    phases change.  So (1) with cuSOLVER's vectors given the phases of the
+    refined ones, the updates agree to 1e-10 or 10x the conditioning floor
+    (the change of the cuSOLVER update when every entry of S moves by one
+    ulp), which compares the eigensolvers; (2) as they come, the updates
+    agree to 10x the phase floor (the change of the cuSOLVER update under
+    random phases)."""
     import vmc_jax_gb300 as V
     from vmc_jax_gb300.util import tdvp as T
+    from vmc_jax_gb300.util import gram as G
     L_, M = 32, 128
     rng = np.random.default_rng(0)
     b = rng.normal(0, 0.01, M) + 1j * rng.normal(0, 0.01, M)
@@ -134,33 +141,55 @@ def test_tdvp_two_stage_matches_fp64_eigensolver(cuda):
     td = V.util.TDVP(smp, makeReal="real", rhsPrefactor=1., pinvCutoff=1e-8, snrTol=2, precision="mixed")
     u2, r2, c2 = td._complex_rhs(psi, configs, E, p)
     info = td.refineInfo
-    ev2 = td.ev_c.clone()
+    ev2, U2 = td.ev_c.clone(), td.V.clone()
     keep = T.TDVP.TWO_STAGE_MIN_P
-    gram = td._gram
+    gram, eigh = td._gram, G.eigh_fp64
+    g = torch.Generator(device=cuda).manual_seed(1)
+
+    def phased(ph):
+        def f(A):
+            ev, U = eigh(A)
+            return ev, U * ph(U)[None, :]
+        return f
+
+    def aligned(U):
+        d = (U2.mH @ U).diagonal()
+        return (d / d.abs()).conj()
+
+    def random_phase(U):
+        t = torch.rand(U.shape[1], dtype=torch.float64, device=U.device, generator=g)
+        return torch.polar(torch.ones_like(t), 2 * np.pi * t)
+
+    def perturbed(*a, **k):
+        A = gram(*a, **k)
+        Ep = torch.randn(A.shape, dtype=torch.float64, device=A.device, generator=g)
+        return A + A * (2.0 ** -52 * 0.5 * (Ep + Ep.T))
     try:
         T.TDVP.TWO_STAGE_MIN_P = 1 << 30
         u1, r1, c1 = td._complex_rhs(psi, configs, E, p)
         ev1 = td.ev_c.clone()
-        g = torch.Generator(device=cuda).manual_seed(1)
-
-        def perturbed(*a, **k):
-            A = gram(*a, **k)
-            Ep = torch.randn(A.shape, dtype=torch.float64, device=A.device, generator=g)
-            return A + A * (2.0 ** -52 * 0.5 * (Ep + Ep.T))
+        G.eigh_fp64 = phased(random_phase)
+        uph, _, _ = td._complex_rhs(psi, configs, E, p)
+        G.eigh_fp64 = phased(aligned)
+        ua, _, _ = td._complex_rhs(psi, configs, E, p)
         td._gram = perturbed
-        u0, _, _ = td._complex_rhs(psi, configs, E, p)
+        ua0, _, _ = td._complex_rhs(psi, configs, E, p)
     finally:
         T.TDVP.TWO_STAGE_MIN_P = keep
-        td._gram = gram
-    floor = (torch.linalg.norm(u0 - u1) / torch.linalg.norm(u1)).item()
-    rel = (torch.linalg.norm(u2 - u1) / torch.linalg.norm(u1)).item()
-    print("refinement plan", info, "update difference %.2e, conditioning floor %.2e" % (rel, floor))
+        td._gram, G.eigh_fp64 = gram, eigh
+
+    def rel(x, y):
+        return (torch.linalg.norm(x - y) / torch.linalg.norm(y)).item()
+    floor, phase_floor = rel(ua0, ua), rel(uph, u1)
+    print("refinement plan", info, "update difference: phase-aligned %.2e (conditioning floor %.2e), as computed "
+          "%.2e (phase floor %.2e)" % (rel(u2, ua), floor, rel(u2, u1), phase_floor))
     assert info is not None and info["refined"] is not None
     k = info["refined"]
     lmax = ev1.abs().max().item()
     assert (ev2[-k:] - ev1[-k:]).abs().max().item() / lmax < 1e-12
     assert float(c1) == float(c2)
-    assert rel <= max(1e-10, 10.0 * floor), (rel, floor)
+    assert rel(u2, ua) <= max(1e-10, 10.0 * floor), (rel(u2, ua), floor)
+    assert rel(u2, u1) <= 10.0 * phase_floor, (rel(u2, u1), phase_floor)
 
 
 @pytest.mark.parametrize("cplx", [True, False])
