@@ -274,11 +274,7 @@ class TDVP:
             # conj(A) is A column-major (A Hermitian)
             Acm = torch.conj_physical(A)
             ev, U = self._eigh_fp32(Acm)
-            vtf = self._project(U, f)
-            TIMER.mark("snr")
-            snr = self._snr(data, w, okMean, E, emean, f, U, vtf, status)
-            plan = refine_plan(ev.cpu().numpy(), vtf.cpu().numpy(), snr.cpu().numpy(), self.pinvCutoff,
-                               self.snrTol)
+            plan = refine_plan(ev.cpu().numpy(), None, None, self.pinvCutoff, self.snrTol)
             weight = None
             if plan is not None:
                 TIMER.mark("eigh_refine")
