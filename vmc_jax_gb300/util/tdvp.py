@@ -5,7 +5,7 @@ GPU pipeline:
 
   sample -> fused O_loc -> FP64 mean/variance of E_loc -> FP64 means of O_k
   and force F -> centred data -> Gram contraction S (FP64 / FP32 / mixed
-  BF16x3 on tcgen05) -> FP64 eigendecomposition -> SNR contraction ->
+  BF16x3 on tcgen05) -> eigendecomposition -> SNR contraction ->
   cutoff loop on the device -> update.
 
 The centred data come from the configurations (CpxRBM: O is never stored)
@@ -71,6 +71,7 @@ def transform_helper(x, rhsPrefactor, makeReal):
 REFINE_EXCLUDED_NORM = 1e-6
 REFINE_MAX_FRACTION = 0.5      # refine at most this fraction of the spectrum
 REFINE_MAX_RHO = 0.25          # largest |lambda_excluded / lambda_carrying| accepted
+REFINE_TARGET = 1e-15          # FP32 start error along the rest left after the power steps
 
 
 def solve_weights(ev, vtf, snr, pinvCutoff, snrTol, snrMargin=1.0):
@@ -102,8 +103,8 @@ def refine_plan(ev, vtf, snr, pinvCutoff, snrTol):
     eigenpairs below it may keep FP32 accuracy is decided after the
     refinement, from their share of the update (bulk_weight).  Per power step
     the FP32 error of the refined vectors along the rest (~1e-7 lambda_max /
-    gap) shrinks by rho = lambda_(b-1) / lambda_b.  vtf and snr are not used
-    and kept for the interface."""
+    gap) shrinks by rho = lambda_(b-1) / lambda_b; q steps take it to
+    REFINE_TARGET.  vtf and snr are not used and kept for the interface."""
     n = ev.shape[0]
     a = np.abs(ev)
     lmax = a.max()
@@ -124,7 +125,9 @@ def refine_plan(ev, vtf, snr, pinvCutoff, snrTol):
         return None
     gap = max(a[b] - a[b - 1], 1e-300)
     eps0 = min(1.0, 1e-7 * lmax / gap)
-    q = int(np.ceil(np.log(1e-16 / eps0) / np.log(rho)))
+    # down to REFINE_TARGET: below the 2^-48 (3.6e-15) of the operand
+    # scales to which the Ozaki products themselves are accurate
+    q = int(np.ceil(np.log(REFINE_TARGET / eps0) / np.log(rho)))
     return k, int(min(max(q, 1), 16))
 
 
