@@ -191,3 +191,17 @@ def test_invalid_specs_are_refused_at_submit():
         with pytest.raises(ValueError):
             srv.submit(bad)
     assert srv.states == {}
+
+
+def test_launch_plan_shares_recurring_sets():
+    """A set of ready jobs gets a shared graph from its second launch on;
+    a new set and a single job replay the jobs' own graphs; a set is
+    forgotten with its jobs."""
+    srv = HostServer(hbm_budget=1 << 40)
+    assert srv._launch_plan([2, 1]) == (False, (1, 2))
+    assert srv._launch_plan([1, 2]) == (True, (1, 2))
+    assert srv._launch_plan([3]) == (False, (3,))
+    assert srv._launch_plan([3]) == (False, (3,))
+    assert srv._launch_plan([1, 3]) == (False, (1, 3))
+    srv.graphs[(1, 2)] = object()
+    assert srv._launch_plan([1, 2]) == (True, (1, 2))

@@ -10,11 +10,15 @@ x = 1) or a real-time quench (makeReal='imag', x = i), Euler-integrated.
 * An admitted job's parameters, Markov chains, random-stream counter and
   integrator state stay on the device in persistent per-slot buffers.
 * Each tick launches the sampling + E_loc phase of every job that is ready
-  for its next step as ONE CUDA graph (each job's kernels on its own branch;
-  the graph is captured once per set of ready jobs and replayed), then each
-  job's FP64 solve runs on its own stream from its own host thread, so the
-  solves of different jobs overlap on the GPU, and the next tick samples
-  whichever jobs are ready again.
+  for its next step from CUDA graphs: a set of ready jobs that recurs gets
+  ONE shared graph (each job's kernels on its own branch), a set seen for
+  the first time replays the jobs' own graphs (captured once per job) back
+  to back, so that a mix of short and long steps, whose ready sets rarely
+  repeat, captures nothing per tick.  Captures run in thread-local mode
+  without a device-wide synchronisation: the solves in flight keep running.
+  Then each job's solve runs on its own stream from its own host thread, so
+  the solves of different jobs overlap on the GPU, and the next tick
+  samples whichever jobs are ready again.
 * Per-step latency (graph launch to update applied) and per-job latency
   (arrival to last step) are recorded for p50/p99 reporting.
 * Failures stay with their job: an invalid spec is refused at ``submit``, a
@@ -120,6 +124,7 @@ class _Slot:
         self.step_latencies = []
         self.energies = []
         self.stream = torch.cuda.Stream()
+        self.graph = None            # this job's own sampling + E_loc graph
         L, M = spec.L, spec.M
         dev = global_defs.device()
         rng = np.random.default_rng(spec.seed)
@@ -162,7 +167,7 @@ class _Slot:
         self.sampler.globNumSamples = self.N
         self.theta = self.psi.get_parameters()
 
-    # ---- phase 1: captured into the shared graph
+    # ---- phase 1: captured into the job's own and the shared graphs
     def launch_sampling(self):
         spec = self.spec
         prec = CpxRBM._prec(self.kprec)
@@ -222,7 +227,10 @@ class Server:
         self.queue = []
         self.active = {}
         self.done = {}
-        self.graphs = {}
+        self.graphs = {}             # shared graphs of recurring ready sets
+        self.seen = {}               # ready sets launched so far (several jobs), count
+        self.graph_replays = 0
+        self.shared_replays = 0
         self.lock = threading.Condition()
         self.ready = set()
         self.next_id = 0
@@ -270,21 +278,80 @@ class Server:
         return _Slot(job_id, spec, arrival_wall)
 
     def _launch(self, ids):
-        """Replay the sampling + E_loc graph of the ready jobs ``ids``; returns
-        the event the jobs' solves wait on and the launch time.  A failure
-        while the graph is captured or built has enqueued nothing and raises
-        as it is; a failure of the replay itself may have enqueued part of the
-        jobs' work and raises ``ReplayError``."""
-        g = self._graph_for(ids)
+        """Replay the sampling + E_loc graphs of the ready jobs ``ids``
+        (``_launch_plan``); returns the event the jobs' solves wait on and the
+        launch time.  A failure while a graph is captured has enqueued nothing
+        and raises as it is; a failure of a replay may have enqueued part of
+        the jobs' work and raises ``ReplayError``."""
+        shared, key = self._launch_plan(ids)
+        if shared:
+            if key not in self.graphs:
+                self.graphs[key] = self._capture(key)
+            graphs = [self.graphs[key]]
+        else:
+            graphs = []
+            for jid in key:
+                slot = self.active[jid]
+                if slot.graph is None:
+                    slot.graph = self._capture((jid,))
+                graphs.append(slot.graph)
         t_launch = time.perf_counter()
         try:
-            with torch.cuda.stream(self.sample_stream):
-                g.replay()
-                ev = torch.cuda.Event()
-                ev.record(self.sample_stream)
+            cap = self.sample_stream
+            if shared:
+                with torch.cuda.stream(cap):
+                    graphs[0].replay()
+            else:  # each job's graph from its own (idle) stream, so they run side by side
+                for jid, g in zip(key, graphs):
+                    st = self.active[jid].stream
+                    st.wait_stream(cap)
+                    with torch.cuda.stream(st):
+                        g.replay()
+                for jid in key:
+                    cap.wait_stream(self.active[jid].stream)
+            ev = torch.cuda.Event()
+            ev.record(cap)
         except Exception as e:
             raise ReplayError("%s: %s" % (type(e).__name__, e)) from e
+        self.graph_replays += len(graphs)
+        self.shared_replays += int(shared)
         return ev, t_launch
+
+    def _launch_plan(self, ids):
+        """(shared, key): one shared graph for a set of several jobs seen
+        before (its graph is kept while all its jobs stay), else the jobs'
+        own graphs.  Host logic only."""
+        key = tuple(sorted(ids))
+        if len(key) < 2:
+            return False, key
+        if key in self.graphs:
+            return True, key
+        self.seen[key] = self.seen.get(key, 0) + 1
+        return self.seen[key] >= 2, key
+
+    def _capture(self, ids):
+        """One graph of the sampling + E_loc kernels of the jobs ``ids``,
+        each job on its own stream as a branch of the shared sample stream.
+        Every job in ``ids`` is between steps, so its stream is idle; the
+        capture is thread-local and takes no device-wide synchronisation."""
+        g = torch.cuda.CUDAGraph()
+        cap = self.sample_stream
+        with torch.cuda.stream(cap):
+            g.capture_begin(capture_error_mode="thread_local")
+            try:
+                branches = []
+                for jid in ids:
+                    br = self.active[jid].stream
+                    br.wait_stream(cap)
+                    with torch.cuda.stream(br):
+                        self.active[jid].counters.zero_()
+                        self.active[jid].launch_sampling()
+                    branches.append(br)
+                for br in branches:
+                    cap.wait_stream(br)
+            finally:
+                g.capture_end()
+        return g
 
     def _used(self):
         return sum(footprint_bytes(s.spec) for s in self.active.values())
@@ -319,27 +386,6 @@ class Server:
         self.max_resident = max(self.max_resident, len(self.active))
         return admitted
 
-    def _graph_for(self, ids):
-        key = tuple(sorted(ids))
-        g = self.graphs.get(key)
-        if g is None:
-            torch.cuda.synchronize()
-            g = torch.cuda.CUDAGraph()
-            cap = self.sample_stream
-            with torch.cuda.graph(g, stream=cap, capture_error_mode="thread_local"):
-                branches = []
-                for jid in key:
-                    br = self.active[jid].stream
-                    br.wait_stream(cap)
-                    with torch.cuda.stream(br):
-                        self.active[jid].counters.zero_()
-                        self.active[jid].launch_sampling()
-                    branches.append(br)
-                for br in branches:
-                    cap.wait_stream(br)
-            self.graphs[key] = g
-        return g
-
     def run(self):
         """Serve until every submitted job has finished; returns the report."""
         self.t0 = time.perf_counter()
@@ -365,6 +411,7 @@ class Server:
                     self.states[jid] = "cancelled"
                 ids = [i for i in ids if i not in self.cancelled]
                 self.graphs = {k: v for k, v in self.graphs.items() if all(i in self.active for i in k)}
+                self.seen = {k: v for k, v in self.seen.items() if all(i in self.active for i in k)}
                 if not ids:
                     continue
             try:
@@ -449,6 +496,7 @@ class Server:
                 "step_latency_s": {"p50": percentile(steps, 50), "p99": percentile(steps, 99)},
                 "job_latency_s": {"p50": percentile(jobs, 50), "p99": percentile(jobs, 99)},
                 "max_resident_jobs": self.max_resident, "graph_launches": self.graph_launches,
+                "graph_replays": self.graph_replays, "shared_graph_replays": self.shared_replays,
                 "not_completed": {jid: st for jid, st in self.states.items() if st != "done"}}
 
     def result(self, job_id):
