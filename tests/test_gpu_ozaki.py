@@ -113,3 +113,18 @@ def test_fewer_levels_bound(cuda):
     scale = A.abs().square().sum(0).sqrt()[:, None] * B.abs().square().sum(0).sqrt()[None, :]
     err = ((got - want).abs() / scale).max().item()
     assert err < 2.0 ** -28, err
+
+
+def test_minsr_fp64_tangent_kernel(cuda):
+    """The FP64 MinSR tangent kernel X X^dagger (N = 1280 samples, P = 700)
+    from the Hermitian Ozaki product: exactly Hermitian, entries within 2^-48
+    of the row / column scales of cuBLAS ZGEMM's X X^dagger."""
+    from vmc_jax_gb300.util.minsr import tangent_kernel_fp64
+    g = torch.Generator(device=cuda).manual_seed(11)
+    X = torch.randn(1280, 700, dtype=torch.complex128, device=cuda, generator=g)
+    T = tangent_kernel_fp64(X)
+    want = X @ X.mH
+    nrm = X.abs().square().sum(1).sqrt()
+    err = ((T - want).abs() / (nrm[:, None] * nrm[None, :])).max().item()
+    assert err < 2.0 ** -48, err
+    assert torch.equal(T, T.mH.resolve_conj())

@@ -62,6 +62,7 @@ def mixed_snr_colsq(data, w, okMean, E, emean, f, U, x, status=None, products=3)
 
 
 OZAKI_MIN_DIM = 1024   # below this the FP64 product goes through cuBLAS
+OZAKI_MAX_K = 30720    # longest complex reduction of vmc_zgemm_ozaki (int64 tile sums below 2^63)
 
 
 def fp64_product(trans_a, A, lda, trans_b, B, ldb, m, n, k, hermitian=False, status=None):

@@ -39,6 +39,19 @@ def pinv_apply(factors, x):
     return V @ (inv.to(V.dtype) * (V.mH @ x))
 
 
+def tangent_kernel_fp64(X):
+    """X X^dagger (N x N) of complex128 samples X (N x P, row-major): the
+    FP64-accurate Hermitian tensor-core product (vmc_zgemm_ozaki) for
+    N >= 1024 and P within its reduction limit, cuBLAS ZGEMM below."""
+    from . import gram as _gram
+    N, P = X.shape
+    if N < _gram.OZAKI_MIN_DIM or P > _gram.OZAKI_MAX_K:
+        return X @ X.mH
+    # row-major X is M = X^T column-major (ld P); M^H M = conj(X X^dagger),
+    # whose column-major storage read row-major is X X^dagger
+    return _gram.fp64_product("C", X, P, "N", X, P, N, N, P, hermitian=True)
+
+
 def tangent_kernel_mixed(X):
     """X X^dagger (N x N complex128) of complex samples X (N x P) on the
     tcgen05 Gram kernel: rows [Re X; Im X] as BF16 hi/lo planes, FP32
@@ -147,7 +160,7 @@ class MinSR:
         if self.precision == "mixed":
             T = 2.0 * tangent_kernel_mixed(X)
         else:
-            T = (2.0 * (X @ X.mH)).to(torch.complex128)
+            T = 2.0 * (tangent_kernel_fp64(X) if self.precision == "fp64" else (X @ X.mH).to(torch.complex128))
         e = torch.sqrt(w).to(torch.complex128) * (E - emean[0])
         v = pinv_apply(pinv_hermitian(T, self.pinvTol), e)
         wv = X.to(torch.complex128).mH @ v     # g^dagger T^+ e  (P)

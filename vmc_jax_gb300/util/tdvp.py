@@ -462,7 +462,7 @@ class TDVP:
         X = torch.empty((data.N, data.P), dtype=dt, device=data.device)
         data.centered(w, okMean, fmt, X, None, data.P)
         N, P = data.N, data.P
-        if self.precision == "fp64" and P >= _gram.OZAKI_MIN_DIM:
+        if self.precision == "fp64" and P >= _gram.OZAKI_MIN_DIM and N <= _gram.OZAKI_MAX_K:
             # X row-major (N x P) is M = X^T column-major; M M^H = conj(A),
             # whose column-major storage read row-major is A
             A = _gram.fp64_product("N", X, P, "C", X, P, P, P, N, hermitian=True, status=status)
@@ -488,7 +488,7 @@ class TDVP:
             fmt, dt = (0, torch.complex128) if self.precision == "fp64" else (1, torch.complex64)
             H = torch.empty((data.N, P), dtype=dt, device=dev)
             data.snr_data(w, okMean, E, emean, -x, f, fmt, H, None, P)
-            if self.precision == "fp64" and P >= _gram.OZAKI_MIN_DIM and U.stride(0) == 1:
+            if self.precision == "fp64" and P >= _gram.OZAKI_MIN_DIM and P <= _gram.OZAKI_MAX_K and U.stride(0) == 1:
                 # Y^T = U^H H^T (P x N column-major) is Y (N x P) row-major
                 Y = _gram.fp64_product("C", U, U.stride(1), "N", H, P, P, data.N, P, status=status)
             else:
