@@ -72,8 +72,8 @@ def parse():
     ap.add_argument("--quench", type=float, default=None,
                     help="XXZ L=48 real-time quench with the adaptive Heun integrator up to this time: energy drift "
                          "of the mixed form and of the FP64 form")
-    ap.add_argument("--quench-steps", type=int, default=40, help="step cap of each quench integration")
-    ap.add_argument("--quench-wall", type=float, default=240.0, help="wall-clock cap (s) of each quench integration")
+    ap.add_argument("--quench-steps", type=int, default=100, help="step cap of each quench integration")
+    ap.add_argument("--quench-wall", type=float, default=600.0, help="wall-clock cap (s) of each quench integration")
     ap.add_argument("--kernel", default=None,
                     choices=["gram", "snr", "eloc", "metropolis", "data", "hermitian", "gemv", "stats"],
                     help="time one kernel on a fixed synthetic case instead of the TDVP step (profiling)")
