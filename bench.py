@@ -7,8 +7,9 @@ parameters N(0, 0.01^2) from seed 0; MCSampler with 1024 chains, single
 spin flips, 64 thermalisation sweeps of L proposals, 16 samples per chain
 (N_s = 16,384); TDVP imaginary time (makeReal='real', rhsPrefactor=1,
 pinvCutoff=1e-8, snrTol=2) in the mixed form (FP32 sampling / E_loc
-kernels, BF16x3 tcgen05 S and SNR contractions, FP64 statistics and FP64
-eigendecomposition); one Euler step dtau = 0.01 per step.  Inputs are
+kernels, BF16x3 tcgen05 S and SNR contractions, FP64 statistics, FP32
+eigendecomposition with the eigenpairs that carry the solve refined to FP64
+accuracy, FP64 solve); one Euler step dtau = 0.01 per step.  Inputs are
 synthetic and seeded; there is no dataset.
 
 ``--impl reference`` times the CPU restatement of jVMC's algorithm (the
