@@ -104,25 +104,10 @@ def test_refinement_improves_fp32_vectors(cuda):
     assert e32 > 1e-10 and e < 1e-13, (e32, e)
 
 
-def test_tdvp_two_stage_matches_fp64_eigensolver(cuda):
-    """The mixed TDVP step with the two-stage eigensolver against the same
-    step with cuSOLVER's FP64 eigendecomposition of the same S, on the same
-    Monte Carlo samples (TFIM L=32, h=1, CpxRBM M=128, 4096 samples; 528 of
-    4224 eigenpairs above the spectral gap).  The refined block must carry
-    the solve and its eigenvalues agree to 1e-12 of the largest.
-
-    Each eigenvector is fixed only up to a phase, and the mixed form's
-    per-eigenvector SNR (tdvp.py:173-181) is a BF16x3 contraction whose
-    rounding depends on that phase: the update moves by ~1e-7 when the
-    phases change.  So (1) with cuSOLVER's vectors given the phases of the
-    refined ones, the updates agree to 1e-10 or 10x the conditioning floor
-    (the change of the cuSOLVER update when every entry of S moves by one
-    ulp), which compares the eigensolvers; (2) as they come, the updates
-    agree to 10x the phase floor (the change of the cuSOLVER update under
-    random phases)."""
+def _mc_workload():
+    """TFIM L=32, h=1, CpxRBM M=128 (4224 complex parameters), 512 chains x 8
+    = 4096 Monte Carlo samples; the mixed-form TDVP solver."""
     import vmc_jax_gb300 as V
-    from vmc_jax_gb300.util import tdvp as T
-    from vmc_jax_gb300.util import gram as G
     L_, M = 32, 128
     rng = np.random.default_rng(0)
     b = rng.normal(0, 0.01, M) + 1j * rng.normal(0, 0.01, M)
@@ -139,6 +124,28 @@ def test_tdvp_two_stage_matches_fp64_eigensolver(cuda):
     configs, _, p = smp.sample()
     E = H.get_O_loc_fused(configs, psi, None, 0.)
     td = V.util.TDVP(smp, makeReal="real", rhsPrefactor=1., pinvCutoff=1e-8, snrTol=2, precision="mixed")
+    return psi, configs, E, p, td
+
+
+def test_tdvp_two_stage_matches_fp64_eigensolver(cuda):
+    """The mixed TDVP step with the two-stage eigensolver against the same
+    step with cuSOLVER's FP64 eigendecomposition of the same S, on the same
+    Monte Carlo samples (TFIM L=32, h=1, CpxRBM M=128, 4096 samples; 528 of
+    4224 eigenpairs above the spectral gap).  The refined block must carry
+    the solve and its eigenvalues agree to 1e-12 of the largest.
+
+    Each eigenvector is fixed only up to a phase, and the mixed form's
+    per-eigenvector SNR (tdvp.py:173-181) is a BF16x3 contraction whose
+    rounding depends on that phase: the update moves by ~1e-7 when the
+    phases change.  So (1) with cuSOLVER's vectors given the phases of the
+    refined ones, the updates agree to 1e-10 or 10x the conditioning floor
+    (the change of the cuSOLVER update when every entry of S moves by one
+    ulp), which compares the eigensolvers; (2) as they come, the updates
+    agree to 10x the phase floor (the change of the cuSOLVER update under
+    random phases)."""
+    from vmc_jax_gb300.util import tdvp as T
+    from vmc_jax_gb300.util import gram as G
+    psi, configs, E, p, td = _mc_workload()
     u2, r2, c2 = td._complex_rhs(psi, configs, E, p)
     info = td.refineInfo
     ev2, U2 = td.ev_c.clone(), td.V.clone()
@@ -207,3 +214,21 @@ def test_fp64_eigensolver_matches_torch(cuda, cplx):
     assert (ev - ref).abs().max().item() / ref.abs().max().item() < 1e-13
     R = A @ U - U * ev[None, :].to(dt)
     assert R.abs().max().item() / ref.abs().max().item() < 1e-12
+
+
+def test_tdvp_falls_back_when_the_refinement_fails(cuda, monkeypatch):
+    """A Rayleigh-Ritz step that fails (X^H X not positive definite) sends
+    the step to the FP64 eigensolver of the whole S: the update is then the
+    FP64 path's, bit for bit, and the solver records why."""
+    from vmc_jax_gb300.util import tdvp as T
+    psi, configs, E, p, td = _mc_workload()
+    keep = T.TDVP.TWO_STAGE_MIN_P
+    try:
+        T.TDVP.TWO_STAGE_MIN_P = 1 << 30
+        u1, _, _ = td._complex_rhs(psi, configs, E, p)
+    finally:
+        T.TDVP.TWO_STAGE_MIN_P = keep
+    monkeypatch.setattr(T.TDVP, "_eigh_refine", lambda self, *a, **k: False)
+    u2, _, _ = td._complex_rhs(psi, configs, E, p)
+    assert td.refineInfo["refined"] is None and td.refineInfo["fallback"] == "Rayleigh-Ritz failed"
+    assert torch.equal(u1, u2)

@@ -65,3 +65,16 @@ def test_solve_weights_match_the_regulariser():
     ref = np.abs(vtf) / ev / (1 + (1e-8 / r) ** 6) / (1 + (2 / snr) ** 6)
     ref[r <= 1e-14] = 0.0
     np.testing.assert_allclose(w, ref, rtol=1e-14, atol=0)
+
+
+def test_plan_refuses_steps_that_collapse_the_block():
+    """A refined block spanning 1e-3 .. 1 of lambda_max needs 4 power steps
+    here (rho 1e-3); they would grow the FP32 mixing inside the block by
+    (1e3)^4, beyond REFINE_MAX_GROWTH, so the plan is refused.  A block
+    spanning 0.05 .. 1 needs 3 steps and grows it by 20^3 = 8000."""
+    rng = np.random.default_rng(3)
+    wide = np.sort(np.concatenate([10.0 ** rng.uniform(-10, -6, 800), [1e-3], rng.uniform(1e-3, 1.0, 199)]))
+    assert T.refine_plan(wide, None, None, 1e-8, 2) is None
+    narrow = _spectrum(rng, 0, 800, 200)
+    k, q = T.refine_plan(narrow, None, None, 1e-8, 2)
+    assert (k, q) == (200, 3) and (narrow.max() / narrow[800]) ** q < T.REFINE_MAX_GROWTH

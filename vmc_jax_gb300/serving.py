@@ -497,7 +497,8 @@ class Server:
                 "job_latency_s": {"p50": percentile(jobs, 50), "p99": percentile(jobs, 99)},
                 "max_resident_jobs": self.max_resident, "graph_launches": self.graph_launches,
                 "graph_replays": self.graph_replays, "shared_graph_replays": self.shared_replays,
-                "not_completed": {jid: st for jid, st in self.states.items() if st != "done"}}
+                "not_completed": {jid: st for jid, st in self.states.items() if st != "done"},
+                "errors": {jid: str(msg) for jid, msg in self.errors.items()}}
 
     def result(self, job_id):
         """Final flat parameters and per-step energies of a finished job."""

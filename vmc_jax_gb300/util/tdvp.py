@@ -72,6 +72,14 @@ REFINE_EXCLUDED_NORM = 1e-6
 REFINE_MAX_FRACTION = 0.5      # refine at most this fraction of the spectrum
 REFINE_MAX_RHO = 0.25          # largest |lambda_excluded / lambda_carrying| accepted
 REFINE_TARGET = 1e-15          # FP32 start error along the rest left after the power steps
+# The FP32 mixing (~u32 lambda_max / (lambda_j - lambda_i), ~1e-7) of a
+# larger refined eigenvector j into the column of a smaller one i grows by
+# lambda_j / lambda_i per power step (the steps scale each column by its own
+# 1 / lambda); the growth over the q steps, at most (lambda_max /
+# lambda_b)^q, is kept below 1e5, so that the mixing stays below ~1e-2, the
+# columns far from dependent and the Rayleigh-Ritz Gram matrix X^H X well
+# conditioned.
+REFINE_MAX_GROWTH = 1e5
 
 
 def solve_weights(ev, vtf, snr, pinvCutoff, snrTol, snrMargin=1.0):
@@ -104,7 +112,9 @@ def refine_plan(ev, vtf, snr, pinvCutoff, snrTol):
     refinement, from their share of the update (bulk_weight).  Per power step
     the FP32 error of the refined vectors along the rest (~1e-7 lambda_max /
     gap) shrinks by rho = lambda_(b-1) / lambda_b; q steps take it to
-    REFINE_TARGET.  vtf and snr are not used and kept for the interface."""
+    REFINE_TARGET, and a plan whose steps would grow the mixing inside the
+    refined block by more than REFINE_MAX_GROWTH is refused.  vtf and snr
+    are not used and kept for the interface."""
     n = ev.shape[0]
     a = np.abs(ev)
     lmax = a.max()
@@ -127,8 +137,10 @@ def refine_plan(ev, vtf, snr, pinvCutoff, snrTol):
     eps0 = min(1.0, 1e-7 * lmax / gap)
     # down to REFINE_TARGET: below the 2^-48 (3.6e-15) of the operand
     # scales to which the Ozaki products themselves are accurate
-    q = int(np.ceil(np.log(REFINE_TARGET / eps0) / np.log(rho)))
-    return k, int(min(max(q, 1), 16))
+    q = int(min(max(np.ceil(np.log(REFINE_TARGET / eps0) / np.log(rho)), 1), 16))
+    if q * np.log(lmax / a[b]) > np.log(REFINE_MAX_GROWTH):
+        return None
+    return k, q
 
 
 def bulk_weight(ev, vtf, snr, k, pinvCutoff, snrTol):
@@ -278,17 +290,19 @@ class TDVP:
             Acm = torch.conj_physical(A)
             ev, U = self._eigh_fp32(Acm)
             plan = refine_plan(ev.cpu().numpy(), None, None, self.pinvCutoff, self.snrTol)
-            weight = None
+            weight, fallback = None, None if plan is not None else "no refinement plan"
             if plan is not None:
                 TIMER.mark("eigh_refine")
-                self._eigh_refine(Acm, ev, U, plan[0], plan[1], status)
+                if not self._eigh_refine(Acm, ev, U, plan[0], plan[1], status):
+                    plan, fallback = None, "Rayleigh-Ritz failed"
+            if plan is not None:
                 vtf = self._project(U, f)
                 TIMER.mark("snr")
                 snr = self._snr(data, w, okMean, E, emean, f, U, vtf, status)
                 weight = bulk_weight(ev.cpu().numpy(), vtf.cpu().numpy(), snr.cpu().numpy(), plan[0],
                                      self.pinvCutoff, self.snrTol)
                 if weight > REFINE_EXCLUDED_NORM:
-                    plan = None
+                    plan, fallback = None, "bulk share"
             del Acm
             if plan is None:
                 TIMER.mark("eigh")
@@ -300,7 +314,7 @@ class TDVP:
                 snr = self._snr(data, w, okMean, E, emean, f, U, vtf, status)
             self.refineInfo = {"refined": None if plan is None else plan[0],
                                "power_steps": None if plan is None else plan[1], "n": P,
-                               "fp32_bulk_weight": weight}
+                               "fp32_bulk_weight": weight, "fallback": fallback}
         else:
             if realParams:  # S real symmetric: the real eigensolver, vectors as complex
                 ev, U = _gram_mod().eigh_fp64(A.real.contiguous())
@@ -377,14 +391,16 @@ class TDVP:
 
     def _eigh_refine(self, A, ev, U, k, steps, status):
         """Stage 2: the top k eigenpairs FP64-accurate (vmc_eigh_refine_top);
-        A given column-major."""
+        A given column-major.  False when the Rayleigh-Ritz step failed."""
         P = A.shape[0]
         info = torch.zeros(1, dtype=torch.int32, device=A.device)
         ws = _lib.Workspace.get(_lib.query("vmc_eigh_refine_workspace_bytes", P, k))
         _lib.call("vmc_eigh_refine_top", P, _lib.ptr(A), A.stride(0), k, steps, _lib.ptr(ev), _lib.ptr(U),
                   U.stride(1), _lib.ptr(ws), ws.numel(), _lib.ptr(status), _lib.ptr(info), _lib.stream())
-        if int(info.item()) != 0:
-            raise _lib.VmcError("TDVP: the FP64 Rayleigh-Ritz eigensolver failed (info %d)" % int(info.item()))
+        # info != 0: the k x k generalized eigensolver found X^H X not
+        # positive definite or did not converge; the caller then falls back
+        # to the FP64 eigensolver of the whole matrix
+        return int(info.item()) == 0
 
     def _status_word(self, dev):
         """Device int32 that a tensor-core kernel of this solver sets when one
