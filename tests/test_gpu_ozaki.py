@@ -117,8 +117,11 @@ def test_fewer_levels_bound(cuda):
 
 def test_minsr_fp64_tangent_kernel(cuda):
     """The FP64 MinSR tangent kernel X X^dagger (N = 1280 samples, P = 700)
-    from the Hermitian Ozaki product: exactly Hermitian, entries within 2^-48
-    of the row / column scales of cuBLAS ZGEMM's X X^dagger."""
+    from the Hermitian Ozaki product: exactly Hermitian, entries within 2^-47
+    of the row / column scales of cuBLAS ZGEMM's X X^dagger (the split
+    product's 2^-48 plus the reference's own rounding, ~sqrt(P) u = 3e-15 of
+    the scales on the diagonal, where every term is positive; measured
+    3.9e-15)."""
     from vmc_jax_gb300.util.minsr import tangent_kernel_fp64
     g = torch.Generator(device=cuda).manual_seed(11)
     X = torch.randn(1280, 700, dtype=torch.complex128, device=cuda, generator=g)
@@ -126,5 +129,5 @@ def test_minsr_fp64_tangent_kernel(cuda):
     want = X @ X.mH
     nrm = X.abs().square().sum(1).sqrt()
     err = ((T - want).abs() / (nrm[:, None] * nrm[None, :])).max().item()
-    assert err < 2.0 ** -48, err
+    assert err < 2.0 ** -47, err
     assert torch.equal(T, T.mH.resolve_conj())
