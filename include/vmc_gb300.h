@@ -412,9 +412,12 @@ int vmc_eigh_fp64(int32_t n, int32_t is_complex, const double* A, int64_t lda, d
  * k x k problem H c = theta G c by cuSOLVER zhegvd, V_top = X C).  The other
  * n - k columns of V are made orthogonal to V_top (one Gram-Schmidt pass)
  * and renormalised; their eigenvalues keep the FP32 values.  n <= 30720.
- * *info: zhegvd's status; *status as for the tensor-core kernels.  Replaces
- * the FP64 jnp.linalg.eigh of tdvp.py:157 for the eigenpairs that carry
- * the regularised solve. */
+ * *info: zhegvd's status (> k: X^H X not positive definite, when the power
+ * steps have made the columns nearly dependent -- the ratio
+ * (ev_max / ev_(n-k))^power_steps is too large; the caller then uses
+ * vmc_eigh_fp64 and V is not to be used); *status as for the tensor-core
+ * kernels.  Replaces the FP64 jnp.linalg.eigh of tdvp.py:157 for the
+ * eigenpairs that carry the regularised solve. */
 size_t vmc_eigh_refine_workspace_bytes(int32_t n, int32_t k);
 int vmc_eigh_refine_top(int32_t n, const double* A, int64_t lda, int32_t k, int32_t power_steps, double* ev,
                         double* V, int64_t ldv, void* workspace, size_t workspace_bytes, int32_t* status,
