@@ -896,7 +896,11 @@ def main():
            "config": {**gpu_config(cfg, args.workload, args.precision),
                       "parallelism": "replicas" if world > 1 else "single GPU"},
            "energy": energy, "phase_ms": phases, "gram_kernel_ms": gram_ms, "snr_kernel_ms": snr_ms,
-           "roofline": roofline, "clocks": clock, "gpu_launches": launches, "e2e": e2e}
+           "roofline": roofline, "clocks": clock, "gpu_launches": launches, "e2e": e2e,
+           "notes": ["makeReal='real' SNR: each eigenvalue of S appears twice in the reference's 2P real "
+                     "representation; both members of a pair get the rotation-invariant pair value "
+                     "N |u^H f|^2 / sum_n w_n |u^H (h_n - f)|^2, where the reference's per-eigenvector value "
+                     "depends on LAPACK's basis inside the degenerate pair (tdvp.py:173-181)"]}
     if secondary is not None:
         out["roofline_s_build"] = secondary
     if getattr(ctx["tdvp"], "refineInfo", None) is not None:
