@@ -68,12 +68,14 @@ def test_solve_weights_match_the_regulariser():
 
 
 def test_plan_refuses_steps_that_collapse_the_block():
-    """A refined block spanning 1e-3 .. 1 of lambda_max needs 4 power steps
-    here (rho 1e-3); they would grow the FP32 mixing inside the block by
-    (1e3)^4, beyond REFINE_MAX_GROWTH, so the plan is refused.  A block
-    spanning 0.05 .. 1 needs 3 steps and grows it by 20^3 = 8000."""
+    """Eigenvalues 1e-4 .. 1 of lambda_max above a bulk below 1e-9: the
+    largest relative gap above the FP32 noise floor (4e-6 here) lies inside
+    the top block (~0.005 over 1e-4), whose 7 power steps (rho 0.02) would
+    grow the FP32 mixing inside the block by ~200^7 = 1e16, beyond
+    REFINE_MAX_GROWTH: the plan is refused.  A block spanning 0.05 .. 1 needs
+    3 steps and grows it by 20^3 = 8000."""
     rng = np.random.default_rng(3)
-    wide = np.sort(np.concatenate([10.0 ** rng.uniform(-10, -6, 800), [1e-3], rng.uniform(1e-3, 1.0, 199)]))
+    wide = np.sort(np.concatenate([10.0 ** rng.uniform(-10, -9, 800), [1e-4], rng.uniform(1e-4, 1.0, 199)]))
     assert T.refine_plan(wide, None, None, 1e-8, 2) is None
     narrow = _spectrum(rng, 0, 800, 200)
     k, q = T.refine_plan(narrow, None, None, 1e-8, 2)

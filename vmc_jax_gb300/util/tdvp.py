@@ -72,14 +72,16 @@ REFINE_EXCLUDED_NORM = 1e-6
 REFINE_MAX_FRACTION = 0.5      # refine at most this fraction of the spectrum
 REFINE_MAX_RHO = 0.25          # largest |lambda_excluded / lambda_carrying| accepted
 REFINE_TARGET = 1e-15          # FP32 start error along the rest left after the power steps
-# The FP32 mixing (~u32 lambda_max / (lambda_j - lambda_i), ~1e-7) of a
-# larger refined eigenvector j into the column of a smaller one i grows by
-# lambda_j / lambda_i per power step (the steps scale each column by its own
-# 1 / lambda); the growth over the q steps, at most (lambda_max /
-# lambda_b)^q, is kept below 1e5, so that the mixing stays below ~1e-2, the
-# columns far from dependent and the Rayleigh-Ritz Gram matrix X^H X well
-# conditioned.
-REFINE_MAX_GROWTH = 1e5
+# The FP32 mixing (~u32 lambda_max / (lambda_j - lambda_i), ~6e-8 for the
+# pairs far apart) of a larger refined eigenvector j into the column of a
+# smaller one i grows by lambda_j / lambda_i per power step (the steps scale
+# each column by its own 1 / lambda); over the q steps by at most
+# (lambda_max / lambda_b)^q.  Below 1e10 the mixing stays below ~1e3, the
+# Rayleigh-Ritz Gram matrix X^H X keeps a condition number below ~1e6 and
+# the refined pairs lose at most ~6 of their ~15 digits; far above it the
+# columns become numerically dependent (zhegvd fails, and the step falls
+# back to the FP64 eigensolver).
+REFINE_MAX_GROWTH = 1e10
 
 
 def solve_weights(ev, vtf, snr, pinvCutoff, snrTol, snrMargin=1.0):
