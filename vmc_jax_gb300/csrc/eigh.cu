@@ -19,14 +19,15 @@
 //      caller picks k so that the part of the solve they carry is negligible
 //      (util/tdvp.py: the largest spectral gap above the FP32 noise floor,
 //      and after step 2 the share of the update left on the unrefined
-//      eigenpairs, which must be below 1e-12).
+//      eigenpairs, which must be below 1e-6).
 //
-// cuSOLVER is called through a handle per device and host thread; its
-// device workspace comes from the caller's workspace, its small host
-// workspace from a per-thread buffer.
+// cuSOLVER is called through handles leased from a per-process pool (one
+// per concurrent call and device); its device workspace comes from the
+// caller's workspace, its small host workspace from a per-thread buffer.
 #include <cusolverDn.h>
 
-#include <map>
+#include <cstddef>
+#include <mutex>
 #include <vector>
 
 #include "oz_host.h"
@@ -39,23 +40,71 @@ namespace {
 struct solver_slot {
   cusolverDnHandle_t h = nullptr;
   cusolverDnParams_t p = nullptr;
+  int dev = -1;
 };
 
-int solver_for(cudaStream_t st, solver_slot** out) {
-  static thread_local std::map<int, solver_slot> slots;
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  VMC_REQUIRE(e == cudaSuccess, VMC_ERR_CUDA, "eigh: %s", cudaGetErrorString(e));
-  solver_slot& s = slots[dev];
-  if (!s.h) {
-    VMC_REQUIRE(cusolverDnCreate(&s.h) == CUSOLVER_STATUS_SUCCESS, VMC_ERR_CUDA, "eigh: cusolverDnCreate failed");
-    VMC_REQUIRE(cusolverDnCreateParams(&s.p) == CUSOLVER_STATUS_SUCCESS, VMC_ERR_CUDA,
-                "eigh: cusolverDnCreateParams failed");
-  }
-  VMC_REQUIRE(cusolverDnSetStream(s.h, st) == CUSOLVER_STATUS_SUCCESS, VMC_ERR_CUDA, "eigh: cusolverDnSetStream");
-  *out = &s;
-  return VMC_OK;
+// cuSOLVER handles are created on demand and reused: a call leases a free
+// handle of its device for its duration and gives it back, so host threads
+// that come and go (one per serving step) share a few handles instead of
+// each leaving one behind.  The handles live until the process ends.
+std::mutex& pool_mutex() {
+  static std::mutex m;
+  return m;
 }
+std::vector<solver_slot*>& pool_free() {
+  static std::vector<solver_slot*> v;
+  return v;
+}
+
+class solver_lease {
+ public:
+  solver_lease() = default;
+  solver_lease(const solver_lease&) = delete;
+  solver_lease& operator=(const solver_lease&) = delete;
+  ~solver_lease() {
+    if (s_) {
+      std::lock_guard<std::mutex> g(pool_mutex());
+      pool_free().push_back(s_);
+    }
+  }
+  // A handle of the current device bound to st.
+  int acquire(cudaStream_t st) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    VMC_REQUIRE(e == cudaSuccess, VMC_ERR_CUDA, "eigh: %s", cudaGetErrorString(e));
+    {
+      std::lock_guard<std::mutex> g(pool_mutex());
+      std::vector<solver_slot*>& v = pool_free();
+      for (size_t i = 0; i < v.size(); ++i) {
+        if (v[i]->dev == dev) {
+          s_ = v[i];
+          v.erase(v.begin() + (std::ptrdiff_t)i);
+          break;
+        }
+      }
+    }
+    if (!s_) {
+      solver_slot* n = new solver_slot;
+      n->dev = dev;
+      if (cusolverDnCreate(&n->h) != CUSOLVER_STATUS_SUCCESS) {
+        delete n;
+        VMC_REQUIRE(false, VMC_ERR_CUDA, "eigh: cusolverDnCreate failed");
+      }
+      if (cusolverDnCreateParams(&n->p) != CUSOLVER_STATUS_SUCCESS) {
+        cusolverDnDestroy(n->h);
+        delete n;
+        VMC_REQUIRE(false, VMC_ERR_CUDA, "eigh: cusolverDnCreateParams failed");
+      }
+      s_ = n;
+    }
+    VMC_REQUIRE(cusolverDnSetStream(s_->h, st) == CUSOLVER_STATUS_SUCCESS, VMC_ERR_CUDA, "eigh: cusolverDnSetStream");
+    return VMC_OK;
+  }
+  solver_slot* operator->() const { return s_; }
+
+ private:
+  solver_slot* s_ = nullptr;
+};
 
 std::vector<char>& host_scratch() {
   static thread_local std::vector<char> buf;
@@ -137,8 +186,8 @@ struct refine_layout {
 };
 
 int hegvd_lwork(int k, int* lwork, cudaStream_t st) {
-  solver_slot* s;
-  int rc = solver_for(st, &s);
+  solver_lease s;
+  int rc = s.acquire(st);
   if (rc) return rc;
   VMC_REQUIRE(cusolverDnZhegvd_bufferSize(s->h, CUSOLVER_EIG_TYPE_1, CUSOLVER_EIG_MODE_VECTOR,
                                           CUBLAS_FILL_MODE_UPPER, k, nullptr, k, nullptr, k, nullptr,
@@ -192,8 +241,8 @@ int refine_layout_for(int n, int k, refine_layout& L, cudaStream_t st) {
 }
 
 size_t fp32_device_bytes(int n, cudaStream_t st, size_t* hostBytes) {
-  solver_slot* s;
-  if (solver_for(st, &s)) return 0;
+  solver_lease s;
+  if (s.acquire(st)) return 0;
   size_t dev = 0, host = 0;
   if (cusolverDnXsyevd_bufferSize(s->h, s->p, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, CUDA_C_32F,
                                   nullptr, n, CUDA_R_32F, nullptr, CUDA_C_32F, &dev, &host) != CUSOLVER_STATUS_SUCCESS)
@@ -234,8 +283,8 @@ extern "C" int vmc_eigh_fp32(int32_t n, const double* A, int64_t lda, double* ev
   to_c64_kernel<<<grid_for(total), 256, 0, st>>>(reinterpret_cast<const double2*>(A), lda, n, A32);
   int rc = check_launch("vmc_eigh_fp32(convert)");
   if (rc) return rc;
-  solver_slot* s;
-  if ((rc = solver_for(st, &s))) return rc;
+  solver_lease s;
+  if ((rc = s.acquire(st))) return rc;
   std::vector<char>& hb = host_scratch();
   if (hb.size() < hostBytes + 1) hb.resize(hostBytes + 1);
   const cusolverStatus_t cs =
@@ -321,8 +370,8 @@ extern "C" int vmc_eigh_refine_top(int32_t n, const double* A, int64_t lda, int3
   if ((rc = oz_finish(out, opC, opB, true, H, k, false, st, 1.0))) return rc;
 
   // H c = theta G c in FP64
-  solver_slot* s;
-  if ((rc = solver_for(st, &s))) return rc;
+  solver_lease s;
+  if ((rc = s.acquire(st))) return rc;
   int lwork = 0;
   if ((rc = hegvd_lwork(k, &lwork, st))) return rc;
   const cusolverStatus_t cs = cusolverDnZhegvd(
@@ -377,8 +426,8 @@ extern "C" int vmc_eigh_refine_top(int32_t n, const double* A, int64_t lda, int3
 namespace vmc {
 namespace {
 size_t fp64_device_bytes(int n, int cplx, cudaStream_t st, size_t* hostBytes) {
-  solver_slot* s;
-  if (solver_for(st, &s)) return 0;
+  solver_lease s;
+  if (s.acquire(st)) return 0;
   size_t dev = 0, host = 0;
   const cudaDataType ta = cplx ? CUDA_C_64F : CUDA_R_64F;
   if (cusolverDnXsyevd_bufferSize(s->h, s->p, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, ta, nullptr, n,
@@ -415,8 +464,8 @@ extern "C" int vmc_eigh_fp64(int32_t n, int32_t is_complex, const double* A, int
                                       cudaMemcpyDeviceToDevice, st);
     VMC_REQUIRE(e == cudaSuccess, VMC_ERR_CUDA, "vmc_eigh_fp64: %s", cudaGetErrorString(e));
   }
-  solver_slot* s;
-  int rc = solver_for(st, &s);
+  solver_lease s;
+  int rc = s.acquire(st);
   if (rc) return rc;
   std::vector<char>& hb = host_scratch();
   if (hb.size() < hostBytes + 1) hb.resize(hostBytes + 1);
