@@ -172,3 +172,17 @@ def test_distribute_sampling():
     assert mpi.distribute_sampling(1000, localDevices=1, numChainsPerDevice=777) == (2, 1554)
     assert mpi.distribute_sampling(1024) == (1024, 1024)
     assert mpi.globNumSamples == 1024
+
+
+def test_launch_accounting_of_the_refinement():
+    """The host's count of the kernels one vmc_eigh_refine_top call launches
+    (the bench line's gpu_launches) against the ncu launch list of the
+    64-site step: n = 16,640, k = 2080, 3 power steps, 4 orthogonalisation
+    chunks -> 19 operand slicings (each a row-exponent and a slice kernel),
+    15 Ozaki products, 15 assemblies, 3 column scalings, 1 normalisation."""
+    n, k, q = 16640, 2080, 3
+    assert L._refine_launches((n, None, None, k, q)) == 2 * 19 + 15 + 15 + 3 + 1
+    # an odd reduction length adds the padding kernel to every slicing of that operand
+    assert L._slice_launches(16641) == 3 and L._slice_launches(16640) == 2
+    # an Ozaki product: both operands sliced, one product, one assembly
+    assert L.KERNELS_PER_CALL["vmc_zgemm_ozaki"]((ord("C"), ord("N"), 4096, 4096, 4096)) == 2 * 2 + 2

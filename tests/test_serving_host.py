@@ -114,6 +114,7 @@ def test_failure_stays_with_its_job():
     assert srv.status(bad) == "failed" and "planted failure" in srv.errors[bad]
     assert all(srv.status(i) == "done" for i in good)
     assert rep["jobs"] == 3 and rep["steps"] == 12
+    assert "planted failure" in rep["errors"][bad] and set(rep["errors"]) == {bad}
 
 
 class LaunchFailServer(HostServer):
